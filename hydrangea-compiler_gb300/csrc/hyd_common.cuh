@@ -1,0 +1,163 @@
+// hyd_common.cuh -- shared internals of the sm_103a runtime: status/error
+// plumbing, the per-device context with per-stream scratch workspaces, and the
+// device-side helpers (256-bit streaming loads, counter-based RNG) that every
+// kernel file uses.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+
+#include "hyd_cuda.h"
+
+namespace hyd {
+
+// ---------------------------------------------------------------- errors ----
+int set_error(int status, const char* fmt, ...);
+const char* last_error();
+
+#define HYD_CHECK_ARG(cond, ...)                                  \
+    do {                                                          \
+        if (!(cond)) return ::hyd::set_error(HYD_CUDA_ERR_INVALID, __VA_ARGS__); \
+    } while (0)
+
+#define HYD_CUDA_TRY(expr)                                                         \
+    do {                                                                           \
+        cudaError_t _e = (expr);                                                   \
+        if (_e != cudaSuccess)                                                     \
+            return ::hyd::set_error(_e == cudaErrorMemoryAllocation ? HYD_CUDA_ERR_NOMEM \
+                                                                   : HYD_CUDA_ERR_CUDA, \
+                                    "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                                    __FILE__, __LINE__);                            \
+    } while (0)
+
+#define HYD_TRY(expr)                 \
+    do {                              \
+        int _s = (expr);              \
+        if (_s != HYD_CUDA_OK) return _s; \
+    } while (0)
+
+// Error bits that kernels raise in the per-device error word.
+enum : unsigned {
+    ERRBIT_BOUNDS = 1u,
+    ERRBIT_TIMEOUT = 2u,
+};
+
+// ---------------------------------------------------------------- context ---
+// Scratch memory for one stream.  The first kCounterBytes hold completion
+// counters that kernels leave at zero when they finish; the rest is free-form
+// scratch (partials, flags, tiles) that a kernel may use for one launch.
+struct Workspace {
+    unsigned char* base = nullptr;
+    size_t bytes = 0;
+};
+
+constexpr size_t kCounterBytes = 4096;
+
+struct Device {
+    int id = -1;
+    int sm_count = 0;
+    int max_smem_optin = 0;
+    unsigned* d_err = nullptr;        // error word (device)
+    std::mutex mu;
+    std::unordered_map<cudaStream_t, Workspace> ws;
+    // runtime-owned device buffers (staging for host-pointer entry points)
+    std::unordered_map<std::string, Workspace> bufs;
+    cudaStream_t side[2] = {nullptr, nullptr};  // pipelining streams
+};
+
+// Returns the current device's context, creating it on first use.
+int device(Device** out);
+// Scratch of at least `bytes` beyond the counter area for `stream`.  Growth
+// synchronizes the stream before freeing the old block.
+int workspace(cudaStream_t stream, size_t bytes, unsigned** counters, void** scratch);
+
+// Runtime-owned device buffer named `key` of at least `bytes` (grows; the
+// caller must not have work in flight on an old block when it grows).
+int device_buffer(Device* d, const char* key, size_t bytes, void** p);
+// The two non-blocking streams host-pointer entry points pipeline on.
+int side_streams(Device* d, cudaStream_t out[2]);
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Kernel launch error check after a <<<>>> launch.
+inline int launch_check(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(HYD_CUDA_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+    return HYD_CUDA_OK;
+}
+
+// ------------------------------------------------------------ device helpers
+// SplitMix64 output function over a Weyl sequence indexed by element number
+// (Steele, Lea, Flood, OOPSLA 2014); identical to the oracle's generator.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+__host__ __device__ __forceinline__ uint64_t rand_u64(uint64_t seed_mixed, uint64_t i) {
+    return mix64(seed_mixed + (i + 1ULL) * 0x9E3779B97F4A7C15ULL);
+}
+
+struct f64x4 { double x, y, z, w; };
+struct u64x4 { unsigned long long x, y, z, w; };
+
+// 256-bit read-only streaming loads (sm_100+ `ld.global.nc.v4.b64`), no L1
+// allocation: each input byte is read exactly once.
+__device__ __forceinline__ f64x4 ldg_stream_f64x4(const double* p) {
+    f64x4 r;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.f64 {%0,%1,%2,%3}, [%4];"
+                 : "=d"(r.x), "=d"(r.y), "=d"(r.z), "=d"(r.w)
+                 : "l"(p));
+    return r;
+}
+__device__ __forceinline__ u64x4 ldg_stream_u64x4(const void* p) {
+    u64x4 r;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.u64 {%0,%1,%2,%3}, [%4];"
+                 : "=l"(r.x), "=l"(r.y), "=l"(r.z), "=l"(r.w)
+                 : "l"(p));
+    return r;
+}
+__device__ __forceinline__ void stg_f64x4(double* p, f64x4 v) {
+    asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(p), "d"(v.x), "d"(v.y), "d"(v.z),
+                 "d"(v.w)
+                 : "memory");
+}
+
+__device__ __forceinline__ void raise_error(unsigned* err, unsigned bit) { atomicOr(err, bit); }
+
+// Divide/remainder by a runtime-invariant positive int64 divisor with C's
+// truncating semantics.  Power-of-two divisors use shifts/masks; others fall
+// back to the hardware-emulated 64-bit divide.
+struct DivMod64 {
+    long long d;
+    unsigned long long mask;
+    int shift;  // >= 0 when d is a power of two
+    __host__ void init(long long dv) {
+        d = dv;
+        shift = -1;
+        mask = 0;
+        if (dv > 0 && (dv & (dv - 1)) == 0) {
+            int s = 0;
+            while ((1LL << s) != dv) ++s;
+            shift = s;
+            mask = (unsigned long long)dv - 1ULL;
+        }
+    }
+    __device__ __forceinline__ long long rem(long long x) const {
+        if (shift >= 0) {
+            if (x >= 0) return (long long)((unsigned long long)x & mask);
+            // C: the remainder takes the sign of the dividend.
+            return -(long long)((0ULL - (unsigned long long)x) & mask);
+        }
+        return x % d;
+    }
+};
+
+}  // namespace hyd

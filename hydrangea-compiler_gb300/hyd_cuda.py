@@ -1,0 +1,201 @@
+"""Python mirror of the libhyd_cuda.so C ABI (include/hyd_cuda.h).
+
+This is the host-side binding the tests and ``bench.py`` use.  It calls the
+C entry points through ctypes with plain pointers; device buffers are torch
+CUDA tensors (torch is only the allocator/stream plumbing here) and streams are
+passed as their raw ``cudaStream_t``.  There is no CPU fallback: if the
+library is missing, importing this module raises.
+"""
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhyd_cuda.so")
+HEADER_DIR = os.path.join(os.path.dirname(HERE), "include")
+
+OK = 0
+ERR_INVALID, ERR_NOMEM, ERR_CUDA, ERR_NO_DEVICE, ERR_BOUNDS = 1, 2, 3, 4, 5
+ERR_TIMEOUT, ERR_BUDGET, ERR_CANCELLED, ERR_UNSUPPORTED = 6, 7, 8, 9
+
+SCATTER_AUTO, SCATTER_SMEM_WARP, SCATTER_SMEM_BLOCK, SCATTER_CLUSTER, SCATTER_GLOBAL = 0, 1, 2, 3, 4
+
+_p = C.c_void_p
+_i64 = C.c_int64
+_u64 = C.c_uint64
+_d = C.c_double
+_i = C.c_int
+
+# name -> (restype, argtypes); every function declared in include/*.h that the
+# Python side calls is listed here.
+SIGNATURES = {
+    "hyd_cuda_init": (_i, []),
+    "hyd_cuda_cleanup": (None, []),
+    "hyd_cuda_last_error": (C.c_char_p, []),
+    "hyd_cuda_status_string": (C.c_char_p, [_i]),
+    "hyd_cuda_version": (_i, []),
+    "hyd_cuda_device_sm_count": (_i, []),
+    "hyd_cuda_check": (_i, [_p]),
+    "hyd_cuda_fill_uniform_f64": (_i, [_p, _i64, _u64, _d, _d, _p]),
+    "hyd_cuda_fill_uniform_i64": (_i, [_p, _i64, _u64, _i64, _p]),
+    "hyd_cuda_dot_f64": (_i, [_p, _p, _i64, _p, _p]),
+    "hyd_cuda_sum_f64": (_i, [_p, _i64, _p, _p]),
+    "hyd_cuda_weighted_histogram_i64": (_i, [_p, _i64, _i64, _p, _i, _p]),
+    "hyd_cuda_scatter_add_i64": (_i, [_p, _p, _i64, _p, _i64, _i, _p]),
+    "hyd_cuda_scatter_add_f64": (_i, [_p, _p, _i64, _p, _i64, _p]),
+    "hyd_cuda_weighted_histogram_host": (_i, [_p, _i64, _i64, _p, _i]),
+    "hyd_cuda_dot_f64_host": (_i, [_p, _p, _i64, _p]),
+    "hyd_cuda_array_alloc": (_p, [None, C.c_size_t]),
+    "hyd_export_weighted_histogram": (_p, [_p, _i64]),
+    "hyd_export_dot": (_d, [_p, _p]),
+}
+
+
+class Tuple(C.Structure):
+    """hyd_tuple_t (runtime/hydrangea_runtime.h:220-223)."""
+    _fields_ = [("elems", C.c_int64 * 8), ("ndims", C.c_int)]
+
+
+class Storage(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("refcount", C.c_int64)]
+
+
+class Array(C.Structure):
+    """hyd_array_t (runtime/hydrangea_runtime.h:230-235)."""
+    _fields_ = [("storage", C.POINTER(Storage)), ("data", C.c_void_p), ("elem_size", C.c_size_t),
+                ("shape", Tuple)]
+
+
+class HydCudaError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("hyd_cuda status %d: %s" % (status, msg))
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libhyd_cuda.so is not built (run __graft_entry__.build())")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            args = [Tuple if a is None else a for a in args]
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def header_functions():
+    """Names of all functions declared in include/*.h."""
+    names = []
+    for f in sorted(os.listdir(HEADER_DIR)):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(HEADER_DIR, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"\b(hyd_[A-Za-z0-9_]+)\s*\(", text):
+            if m.group(1) not in names:
+                names.append(m.group(1))
+    return names
+
+
+def last_error():
+    return (lib().hyd_cuda_last_error() or b"").decode()
+
+
+def check(status):
+    if status != OK:
+        raise HydCudaError(status, last_error())
+    return status
+
+
+def ptr(t):
+    """Raw device pointer of a torch tensor (or an int pointer)."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    return t.data_ptr()
+
+
+def stream_handle(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def call(name, *args):
+    return check(getattr(lib(), name)(*args))
+
+
+# ---- convenience wrappers over torch tensors -----------------------------------
+
+def fill_uniform_f64(out, seed, lo, hi, stream=None):
+    call("hyd_cuda_fill_uniform_f64", ptr(out), out.numel(), seed, lo, hi, stream_handle(stream))
+
+
+def fill_uniform_i64(out, seed, bound, stream=None):
+    call("hyd_cuda_fill_uniform_i64", ptr(out), out.numel(), seed, bound, stream_handle(stream))
+
+
+def dot_f64(xs, ys, out, stream=None):
+    call("hyd_cuda_dot_f64", ptr(xs), ptr(ys), xs.numel(), ptr(out), stream_handle(stream))
+
+
+def sum_f64(xs, out, stream=None):
+    call("hyd_cuda_sum_f64", ptr(xs), xs.numel(), ptr(out), stream_handle(stream))
+
+
+def weighted_histogram(data, hist, strategy=SCATTER_AUTO, stream=None):
+    call("hyd_cuda_weighted_histogram_i64", ptr(data), data.numel(), hist.numel(), ptr(hist),
+         strategy, stream_handle(stream))
+
+
+def scatter_add_i64(idx, vals, dst, strategy=SCATTER_AUTO, stream=None):
+    call("hyd_cuda_scatter_add_i64", ptr(idx), ptr(vals), idx.numel(), ptr(dst), dst.numel(),
+         strategy, stream_handle(stream))
+
+
+def scatter_add_f64(idx, vals, dst, stream=None):
+    call("hyd_cuda_scatter_add_f64", ptr(idx), ptr(vals), idx.numel(), ptr(dst), dst.numel(),
+         stream_handle(stream))
+
+
+def make_array(np_array):
+    """A hyd_array_t view of a C-contiguous numpy array (no copy; storage is
+    borrowed, so never pass it to hyd_array_free)."""
+    st = Storage(np_array.ctypes.data, 1)
+    t = Tuple()
+    t.ndims = np_array.ndim
+    for i, e in enumerate(np_array.shape):
+        t.elems[i] = e
+    a = Array(C.pointer(st), np_array.ctypes.data, np_array.itemsize, t)
+    a._keep = (st, np_array)
+    return a
+
+
+def weighted_histogram_host(data, bins, strategy=SCATTER_AUTO):
+    import numpy as np
+    data = np.ascontiguousarray(data, dtype=np.int64)
+    out = np.zeros(bins, dtype=np.int64)
+    call("hyd_cuda_weighted_histogram_host", data.ctypes.data, data.size, bins, out.ctypes.data, strategy)
+    return out
+
+
+def dot_f64_host(xs, ys):
+    import numpy as np
+    xs = np.ascontiguousarray(xs, dtype=np.float64)
+    ys = np.ascontiguousarray(ys, dtype=np.float64)
+    r = C.c_double(0.0)
+    call("hyd_cuda_dot_f64_host", xs.ctypes.data, ys.ctypes.data, xs.size, C.addressof(r))
+    return r.value
+
+
+def device_check(stream=None):
+    return lib().hyd_cuda_check(stream_handle(stream))

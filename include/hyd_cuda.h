@@ -1,0 +1,149 @@
+/* include/hyd_cuda.h -- C ABI of the GB300 (sm_103a) CUDA runtime for the
+ * Hydrangea fused-loop hot path.
+ *
+ * Two layers:
+ *   1. Device primitives on raw device pointers and a CUDA stream (cudaStream_t
+ *      passed as void*; NULL = the legacy default stream).  These are the calls
+ *      that host code generated for `--backend cuda` makes for each fused loop
+ *      nest, one per loop template of the reference C backend.
+ *   2. The embedding boundary on `hyd_array_t*` (the reference runtime's array
+ *      ABI, unchanged): lifecycle `hyd_cuda_init` / `hyd_cuda_cleanup` in the
+ *      style of the Metal backend's exported lifecycle, and `hyd_export_*`
+ *      symbols with the signatures the reference's export wrapper gives the
+ *      benchmark programs.
+ *
+ * Every function returns a hyd_cuda_status_t (0 = success) unless stated
+ * otherwise; hyd_cuda_last_error() describes the most recent failure on the
+ * calling thread.  Argument checks happen before any CUDA call, so a bad call
+ * fails the same way with or without a GPU.
+ *
+ * Reference citations are file:line in hydrangea-compiler.
+ */
+#ifndef HYD_CUDA_H
+#define HYD_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- array ABI -------------------------------------------------------------
+ * Layout-identical to hyd_tuple_t / hyd_array_storage_t / hyd_array_t of
+ * runtime/hydrangea_runtime.h:220-235.  When that header was included first its
+ * definitions are used; otherwise these stand in (the refcount is a plain
+ * int64_t here: same size and alignment as the header's _Atomic int64_t). */
+#ifndef HYDRANGEA_RUNTIME_H
+#define HYD_MAX_DIMS 8
+typedef struct {
+    int64_t elems[HYD_MAX_DIMS];
+    int ndims;
+} hyd_tuple_t;
+typedef struct {
+    unsigned char* data;
+    int64_t refcount;
+} hyd_array_storage_t;
+typedef struct {
+    hyd_array_storage_t* storage;
+    unsigned char* data;
+    size_t elem_size;
+    hyd_tuple_t shape;
+} hyd_array_t;
+#endif
+
+typedef enum {
+    HYD_CUDA_OK = 0,
+    HYD_CUDA_ERR_INVALID = 1,     /* bad argument (null pointer, negative size, ...) */
+    HYD_CUDA_ERR_NOMEM = 2,       /* device or host allocation failed */
+    HYD_CUDA_ERR_CUDA = 3,        /* a CUDA runtime/driver call failed */
+    HYD_CUDA_ERR_NO_DEVICE = 4,   /* no usable GPU */
+    HYD_CUDA_ERR_BOUNDS = 5,      /* a route/index left its destination (device-detected) */
+    HYD_CUDA_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
+    HYD_CUDA_ERR_BUDGET = 7,      /* serving: request exceeds the HBM budget */
+    HYD_CUDA_ERR_CANCELLED = 8,   /* serving: request cancelled or server stopped */
+    HYD_CUDA_ERR_UNSUPPORTED = 9  /* shape/size outside what this build supports */
+} hyd_cuda_status_t;
+
+/* ---- lifecycle (the Metal backend's exported hyd_metal_init/_cleanup pair,
+ *      CodegenMSL.hs:1219-1222, re-targeted at CUDA) ------------------------ */
+int hyd_cuda_init(void);                 /* 0 on success; idempotent */
+void hyd_cuda_cleanup(void);             /* frees runtime-owned device memory */
+const char* hyd_cuda_last_error(void);   /* thread-local message of the last failure */
+const char* hyd_cuda_status_string(int status);
+int hyd_cuda_version(void);              /* ABI version, major*100 + minor */
+int hyd_cuda_device_sm_count(void);      /* SMs of the current device, or -status */
+/* Synchronize `stream`, then report (and clear) device-detected errors such as
+ * out-of-range scatter routes raised by kernels launched since the last check. */
+int hyd_cuda_check(void* stream);
+
+/* ---- seeded synthetic inputs (same counter-based SplitMix64 stream as the
+ *      CPU oracle; element i depends only on (seed, i)) ---------------------- */
+int hyd_cuda_fill_uniform_f64(double* out, int64_t n, uint64_t seed, double lo, double hi,
+                              void* stream);
+int hyd_cuda_fill_uniform_i64(int64_t* out, int64_t n, uint64_t seed, int64_t bound,
+                              void* stream);
+
+/* ---- reduce (+) 0.0 (zipwith (*) xs ys) -----------------------------------
+ * Replaces the parallel reduction template CodegenC.hs:1328-1353 (emitted
+ * `omp parallel for simd reduction(+:acc)`, README.md:25-33) for the fused
+ * reduce_generate of Lowering.hs:771-804.  Deterministic: a fixed grid, per
+ * thread fixed-order accumulation, warp-shuffle trees and a fixed-order final
+ * combine, so the same inputs give the same bits on every run.  *out is a
+ * device pointer to one double. */
+int hyd_cuda_dot_f64(const double* xs, const double* ys, int64_t n, double* out, void* stream);
+/* reduce (+) 0.0 xs, same scheme. */
+int hyd_cuda_sum_f64(const double* xs, int64_t n, double* out, void* stream);
+
+/* ---- scatter (+) ------------------------------------------------------------
+ * Replaces the privatized scatter template CodegenC.hs:1119-1288 and the
+ * atomic template CodegenC.hs:1084-1118 (strategy choice Parallelize.hs:
+ * 466-503).  Fused weighted histogram of examples/weighted_histogram.hyd:
+ *   hist[x % bins] += x * x   for x in data   (int64, wrapping)
+ * `hist` (device, bins int64) is accumulated into, like the reference's
+ * merge into the existing destination; zero it first for `fill [bins] 0`.
+ * A route outside [0, bins) is skipped and reported by hyd_cuda_check. */
+typedef enum {
+    HYD_SCATTER_AUTO = 0,          /* autotuned choice per (bins class) */
+    HYD_SCATTER_SMEM_WARP = 1,     /* per-warp shared-memory bins */
+    HYD_SCATTER_SMEM_BLOCK = 2,    /* one shared-memory copy per block */
+    HYD_SCATTER_CLUSTER = 3,       /* bins spread over a thread-block cluster's DSMEM */
+    HYD_SCATTER_GLOBAL = 4         /* global atomics (bins beyond on-chip memory) */
+} hyd_scatter_strategy_t;
+int hyd_cuda_weighted_histogram_i64(const int64_t* data, int64_t n, int64_t bins,
+                                    int64_t* hist, int strategy, void* stream);
+/* Unfused scatter (+) over materialised routes and values (Lowering.hs:
+ * 1408-1430): dst[idx[i]] += vals[i].  int64 variant is order-independent
+ * (bit-exact); the float variant accumulates with fp64 atomics and is
+ * therefore run-to-run order-dependent within fp64 rounding. */
+int hyd_cuda_scatter_add_i64(const int64_t* idx, const int64_t* vals, int64_t n,
+                             int64_t* dst, int64_t dst_n, int strategy, void* stream);
+int hyd_cuda_scatter_add_f64(const int64_t* idx, const double* vals, int64_t n,
+                             double* dst, int64_t dst_n, void* stream);
+
+/* ---- host-memory entry points (embedding boundary) --------------------------
+ * Same computations on HOST pointers: the input is streamed to the device in
+ * 64 MiB chunks on two streams (copy of chunk k+1 overlaps the kernel on chunk
+ * k) and the result read back.  Synchronous.  `hist` is overwritten with the
+ * result of scatter (+) (fill [bins] 0) ... . */
+int hyd_cuda_weighted_histogram_host(const int64_t* data, int64_t n, int64_t bins, int64_t* hist,
+                                     int strategy);
+int hyd_cuda_dot_f64_host(const double* xs, const double* ys, int64_t n, double* out);
+
+/* Host array allocation compatible with the reference's hyd_array_free
+ * (runtime/hydrangea_runtime.h:292-343): malloc'd header and storage record,
+ * calloc'd data, refcount 1.  NULL on allocation failure. */
+hyd_array_t* hyd_cuda_array_alloc(hyd_tuple_t shape, size_t elem_size);
+
+/* Exported program symbols in the reference's export ABI (CodegenC.hs:
+ * 372-460: `RET hyd_export_<name>(PARAMS)`), for the benchmark programs with
+ * their inputs as parameters.  Like the reference's generated code they print
+ * a message and exit(1) on failure (runtime/hydrangea_runtime.h:322-328).
+ * Returned arrays are owned by the caller (free with hyd_array_free). */
+hyd_array_t* hyd_export_weighted_histogram(hyd_array_t* data, int64_t bins);
+double hyd_export_dot(hyd_array_t* xs, hyd_array_t* ys);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYD_CUDA_H */

@@ -1,0 +1,114 @@
+"""GPU parity: scatter (+) / weighted histogram, bit-exact against the oracle
+for every privatisation strategy, including the workload's bin counts."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+STRATS = ["SCATTER_AUTO", "SCATTER_SMEM_WARP", "SCATTER_SMEM_BLOCK", "SCATTER_CLUSTER", "SCATTER_GLOBAL"]
+
+
+def _data(hc, n, dev, seed=2, bound=1 << 20):
+    d = torch.empty(n, dtype=torch.int64, device=dev)
+    hc.fill_uniform_i64(d, seed, bound)
+    return d
+
+
+def _run(hc, data, bins, strategy, dev):
+    hist = torch.zeros(bins, dtype=torch.int64, device=dev)
+    hc.weighted_histogram(data, hist, strategy=strategy)
+    hc.check(hc.device_check())
+    return hist.cpu().numpy()
+
+
+def test_known_answer_example(hc, orc, dev):
+    data = torch.arange(1024, dtype=torch.int64, device=dev)
+    got = _run(hc, data, 64, hc.SCATTER_AUTO, dev)
+    assert got.tolist() == [sum((k + 64 * j) ** 2 for j in range(16)) for k in range(64)]
+
+
+@pytest.mark.parametrize("bins", [1, 3, 64, 1000, 4096, 65536, 300000])
+@pytest.mark.parametrize("strategy", STRATS)
+def test_strategies_bit_exact(hc, orc, dev, bins, strategy):
+    s = getattr(hc, strategy)
+    data = _data(hc, 200_003, dev)
+    ref = orc.weighted_hist(data.cpu().numpy(), bins)
+    try:
+        got = _run(hc, data, bins, s, dev)
+    except hc.HydCudaError as e:
+        # a forced strategy may not fit this many bins; AUTO always must
+        assert e.status == hc.ERR_UNSUPPORTED and s != hc.SCATTER_AUTO
+        return
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 5, 33, 4099])
+def test_ragged_sizes(hc, orc, dev, n):
+    data = _data(hc, n, dev) if n else torch.empty(0, dtype=torch.int64, device=dev)
+    for bins in (64, 65536):
+        got = _run(hc, data, bins, hc.SCATTER_AUTO, dev)
+        ref = orc.weighted_hist(data.cpu().numpy(), bins) if n else np.zeros(bins, np.int64)
+        assert np.array_equal(got, ref)
+
+
+def test_accumulates_into_existing(hc, orc, dev):
+    data = _data(hc, 10000, dev)
+    hist = torch.arange(64, dtype=torch.int64, device=dev)
+    hc.weighted_histogram(data, hist)
+    ref = orc.weighted_hist(data.cpu().numpy(), 64) + np.arange(64)
+    assert np.array_equal(hist.cpu().numpy(), ref)
+
+
+def test_out_of_range_routes_reported(hc, orc, dev):
+    data = torch.tensor([5, -7, 9, 12], dtype=torch.int64, device=dev)
+    hist = torch.zeros(4, dtype=torch.int64, device=dev)
+    hc.weighted_histogram(data, hist)
+    assert hc.device_check() == hc.ERR_BOUNDS
+    # the in-range routes were still applied: 5%4=1 -> 25, 9%4=1 -> 81, 12%4=0 -> 144
+    assert hist.cpu().tolist() == [144, 106, 0, 0]
+    assert hc.device_check() == hc.OK  # the error word was cleared
+
+
+def test_non_power_of_two_bins_and_wrap(hc, orc, dev):
+    # large values: x*x wraps modulo 2^64 exactly like the oracle's uint64 math
+    data = _data(hc, 50000, dev, seed=9, bound=(1 << 62))
+    for bins in (7, 1000, 65521):
+        assert np.array_equal(_run(hc, data, bins, hc.SCATTER_AUTO, dev),
+                              orc.weighted_hist(data.cpu().numpy(), bins))
+
+
+def test_full_size_workload_both_bin_counts(hc, orc, dev):
+    n = 1 << 27  # the workload's N (1 GiB of int64)
+    data = _data(hc, n, dev)
+    host = data.cpu().numpy()
+    for bins in (64, 65536):
+        got = _run(hc, data, bins, hc.SCATTER_AUTO, dev)
+        assert np.array_equal(got, orc.weighted_hist(host, bins))
+        # size-independent property: the bins sum to sum(x*x) mod 2^64
+        total = int(got.astype(np.uint64).sum(dtype=np.uint64))
+        sq = (host.astype(np.uint64) * host.astype(np.uint64)).sum(dtype=np.uint64)
+        assert total == int(sq)
+
+
+def test_unfused_scatter_add(hc, orc, dev):
+    rng = np.random.default_rng(3)
+    for n, dst_n in ((0, 5), (10, 1), (10007, 64), (10007, 70000)):
+        idx = rng.integers(0, dst_n, size=n).astype(np.int64)
+        vals = rng.integers(-1000, 1000, size=n).astype(np.int64)
+        dst = torch.zeros(dst_n, dtype=torch.int64, device=dev)
+        if n:
+            hc.scatter_add_i64(torch.from_numpy(idx).to(dev), torch.from_numpy(vals).to(dev), dst)
+        hc.check(hc.device_check())
+        assert np.array_equal(dst.cpu().numpy(), orc.scatter_add_i64(idx, vals, dst_n))
+
+
+def test_unfused_scatter_add_f64(hc, orc, dev):
+    rng = np.random.default_rng(4)
+    idx = rng.integers(0, 100, size=5000).astype(np.int64)
+    vals = rng.uniform(-1, 1, size=5000)
+    dst = torch.zeros(100, dtype=torch.float64, device=dev)
+    hc.scatter_add_f64(torch.from_numpy(idx).to(dev), torch.from_numpy(vals).to(dev), dst)
+    ref = np.zeros(100)
+    orc.lib().orc_scatter_add_f64(idx, vals, 5000, ref, 100)
+    assert np.allclose(dst.cpu().numpy(), ref, rtol=1e-12, atol=1e-12)
