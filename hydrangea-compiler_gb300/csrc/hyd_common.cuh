@@ -85,6 +85,10 @@ int side_streams(Device* d, cudaStream_t out[2]);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Sets the maximum dynamic shared memory (and, if asked, non-portable cluster
+// sizes) for kernel `fn` on device `d`, once per (kernel, device).
+int configure_kernel(const void* fn, const Device* d, bool nonportable_cluster);
+
 // Kernel launch error check after a <<<>>> launch.
 inline int launch_check(const char* what) {
     cudaError_t e = cudaGetLastError();

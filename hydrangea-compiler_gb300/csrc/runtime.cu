@@ -111,6 +111,20 @@ int side_streams(Device* d, cudaStream_t out[2]) {
     return HYD_CUDA_OK;
 }
 
+int configure_kernel(const void* fn, const Device* d, bool nonportable_cluster) {
+    static std::mutex mu;
+    static std::unordered_map<const void*, unsigned> done;  // kernel -> device bit mask
+    std::lock_guard<std::mutex> lock(mu);
+    unsigned& mask = done[fn];
+    const unsigned bit = 1u << (d->id & 31);
+    if (mask & bit) return HYD_CUDA_OK;
+    HYD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d->max_smem_optin));
+    if (nonportable_cluster)
+        HYD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    mask |= bit;
+    return HYD_CUDA_OK;
+}
+
 // ------------------------------------------------------------ generators ----
 __global__ void fill_uniform_f64_kernel(double* out, int64_t n, uint64_t seed_mixed, double lo,
                                         double scale) {
