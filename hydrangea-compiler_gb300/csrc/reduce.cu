@@ -162,3 +162,92 @@ extern "C" int hyd_cuda_sum_f64(const double* xs, int64_t n, double* out, void* 
     HYD_CHECK_ARG(n == 0 || xs != nullptr, "sum_f64: null input");
     return reduce_launch(false, xs, nullptr, n, out, as_stream(stream));
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free dot product.
+//
+// Some callers cannot allocate device memory at the point where they need a
+// reduction: a latency-critical serving or real-time loop where cudaMalloc
+// (and the cudaFree that pairs with it) may synchronize the device and stall
+// work on other streams; a process whose device memory was reserved up front
+// by another allocator or capped by a memory policy, where a fresh cudaMalloc
+// can fail at an arbitrary moment; an embedding host that requires a fixed
+// footprint after start-up.  hyd_cuda_dot_f64 takes its scratch (per-CTA
+// partials and a completion counter) from a per-stream workspace that the
+// runtime allocates on first use, so it is not usable there.
+//
+// hyd_cuda_dot_f64_noalloc runs the same kernel with its scratch in the
+// file-scope array below instead.  The array is fixed at load time, so every
+// GPU that loads this library holds these bytes until the process exits.  Its
+// size bounds the launch: kNoAllocMaxBlocks CTAs (two per SM on any GPU with
+// up to 1024 SMs); a launch that would need more is rejected.
+namespace hyd {
+
+constexpr int kNoAllocMaxBlocks = 2048;
+constexpr size_t kNoAllocCounterBytes = 256;
+constexpr size_t kNoAllocScratchBytes = kNoAllocCounterBytes + sizeof(double) * kNoAllocMaxBlocks;
+
+static __device__ __align__(256) unsigned char g_dot_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_dot_noalloc_scratch, looked up once per device with that
+// device current.  In host code the symbol itself is only a host-side stand-in,
+// never a device address, so kernels must be given this pointer.
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_ptr[64] = {nullptr};
+static int g_noalloc_sms[64] = {0};
+
+static int noalloc_setup(int dev, unsigned char** scratch, int* sms) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_dot_noalloc_scratch);
+        if (e != cudaSuccess)
+            return set_error(HYD_CUDA_ERR_CUDA, "dot_f64_noalloc: cudaGetSymbolAddress failed: %s",
+                             cudaGetErrorString(e));
+        int n = 0;
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess)
+            return set_error(HYD_CUDA_ERR_CUDA, "dot_f64_noalloc: SM count query failed: %s",
+                             cudaGetErrorString(e));
+        g_noalloc_sms[dev] = n;
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *scratch = g_noalloc_ptr[dev];
+    *sms = g_noalloc_sms[dev];
+    return HYD_CUDA_OK;
+}
+
+}  // namespace hyd
+
+extern "C" int hyd_cuda_dot_f64_noalloc(const double* xs, const double* ys, int64_t n, double* out,
+                                        void* stream) {
+    HYD_CHECK_ARG(n >= 0, "dot_f64_noalloc: negative length %lld", (long long)n);
+    HYD_CHECK_ARG(out != nullptr, "dot_f64_noalloc: null output");
+    HYD_CHECK_ARG(n == 0 || (xs != nullptr && ys != nullptr), "dot_f64_noalloc: null input");
+    int dev = 0;
+    HYD_CUDA_TRY(cudaGetDevice(&dev));
+    HYD_CHECK_ARG(dev >= 0 && dev < 64, "dot_f64_noalloc: device ordinal %d beyond 63", dev);
+    unsigned char* scratch = nullptr;
+    int sms = 0;
+    HYD_TRY(noalloc_setup(dev, &scratch, &sms));
+    // Same grid rule as hyd_cuda_dot_f64, so both give the same bits.
+    const int64_t units = (n + 3) / 4;
+    int64_t blocks = (int64_t)sms * kRedBlocksPerSM;
+    const int64_t want = (units + 2LL * kRedThreads - 1) / (2LL * kRedThreads);
+    if (want < blocks) blocks = want < 1 ? 1 : want;
+    if (blocks > kNoAllocMaxBlocks)
+        return set_error(HYD_CUDA_ERR_UNSUPPORTED,
+                         "dot_f64_noalloc: needs %lld CTAs of scratch but the static scratch holds %d",
+                         (long long)blocks, kNoAllocMaxBlocks);
+    unsigned* counter = reinterpret_cast<unsigned*>(scratch);
+    double* partials = reinterpret_cast<double*>(scratch + kNoAllocCounterBytes);
+    cudaStream_t st = as_stream(stream);
+    // The array keeps whatever the previous call left; the counter must start at 0.
+    HYD_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+    const bool vec = ((reinterpret_cast<uintptr_t>(xs) | reinterpret_cast<uintptr_t>(ys)) & 31) == 0;
+    if (vec)
+        reduce_f64_kernel<true, true><<<(unsigned)blocks, kRedThreads, 0, st>>>(xs, ys, n, partials, counter, out);
+    else
+        reduce_f64_kernel<true, false><<<(unsigned)blocks, kRedThreads, 0, st>>>(xs, ys, n, partials, counter, out);
+    return launch_check("dot_f64_noalloc");
+}

@@ -40,6 +40,7 @@ SIGNATURES = {
     "hyd_cuda_fill_uniform_i64": (_i, [_p, _i64, _u64, _i64, _p]),
     "hyd_cuda_dot_f64": (_i, [_p, _p, _i64, _p, _p]),
     "hyd_cuda_sum_f64": (_i, [_p, _i64, _p, _p]),
+    "hyd_cuda_dot_f64_noalloc": (_i, [_p, _p, _i64, _p, _p]),
     "hyd_cuda_weighted_histogram_i64": (_i, [_p, _i64, _i64, _p, _i, _p]),
     "hyd_cuda_scatter_add_i64": (_i, [_p, _p, _i64, _p, _i64, _i, _p]),
     "hyd_cuda_scatter_add_f64": (_i, [_p, _p, _i64, _p, _i64, _p]),

@@ -94,6 +94,18 @@ int hyd_cuda_fill_uniform_i64(int64_t* out, int64_t n, uint64_t seed, int64_t bo
 int hyd_cuda_dot_f64(const double* xs, const double* ys, int64_t n, double* out, void* stream);
 /* reduce (+) 0.0 xs, same scheme. */
 int hyd_cuda_sum_f64(const double* xs, int64_t n, double* out, void* stream);
+/* hyd_cuda_dot_f64 for callers that must not allocate device memory (no
+ * counterpart in the reference; it exists for hosts where cudaMalloc may stall
+ * other streams or fail under a fixed memory budget).  Same kernel and same
+ * result bits, but its scratch lives in a static device array inside this
+ * library (about 16 KiB, held on every GPU that loads the library until exit)
+ * instead of a runtime-allocated workspace.  Calls no cudaMalloc/cudaFree and
+ * no allocating library routine.  Limit: at most 2048 CTAs of partials (two per
+ * SM), otherwise HYD_CUDA_ERR_UNSUPPORTED.  The first call on each device looks
+ * up the array's device address; make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU (for
+ * example on two streams at once) race and give wrong results. */
+int hyd_cuda_dot_f64_noalloc(const double* xs, const double* ys, int64_t n, double* out, void* stream);
 
 /* ---- scatter (+) ------------------------------------------------------------
  * Replaces the privatized scatter template CodegenC.hs:1119-1288 and the
