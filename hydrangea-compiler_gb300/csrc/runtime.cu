@@ -182,7 +182,10 @@ int hyd_cuda_init(void) {
     return device(&d);
 }
 
+extern "C" void hyd_cuda_stencil_release_graphs(void);
+
 void hyd_cuda_cleanup(void) {
+    hyd_cuda_stencil_release_graphs();
     std::lock_guard<std::mutex> lock(g_devices_mu);
     int cur = 0;
     if (cudaGetDevice(&cur) != cudaSuccess) cur = 0;

@@ -1,0 +1,372 @@
+// stencil.cu -- 2-D clamp stencils with the 5-point footprint, and `iterate`
+// over them.
+//
+// Replaces the split-region stencil loops of the reference
+// (Lowering.hs:2562-2661 interior + clamped boundary strips, each an
+// `omp parallel for`) and the ping-pong `iterate` of Lowering.hs:840-858 /
+// CFGOpt.hs:795-810.  Per point the body is the program text evaluated left
+// to right (a = acc (-1) 0, b = acc 1 0, c = acc 0 (-1), d = acc 0 1,
+// e = acc 0 0):
+//   LAPLACIAN     a + b + c + d + (e * -4.0)          (bench/stencil/stencil_2d.hyd)
+//   JACOBI        (a + b + c + d) / 4.0                (bench/stencil/jacobi_2d.hyd)
+//   HEAT          e + 0.1 * (a + b + c + d - 4.0 * e)  (the 8192^2 heat step)
+//   HEAT_EXAMPLE  (a + b + c + d + e) / 5.0            (examples/heat_2d.hyd)
+// Results are bit-identical to the C backend: no contraction except where it
+// is exact -- `t3 - 4e` and `t3 + e*-4` are one fma because 4e is exact (for
+// |e| < DBL_MAX/4), and /4.0 is *0.25 (both correctly rounded, same value).
+//
+// GB300 design.  fp64 runs at ~1.9 DFMA/clk/SM on this part, so a 5-point fp64
+// step is bound by the FP64 pipe (6 DP ops per point for HEAT), not by HBM.
+// The kernel therefore spends nothing but DP ops in its inner loop:
+//  * a persistent grid walks 16 x 128 output tiles; each tile plus its halo
+//    (rows -1..+1, columns -2..+2 so the TMA x coordinate stays 16-byte
+//    aligned) is brought into shared memory by a 2-D TMA load
+//    (cp.async.bulk.tensor) completing on an mbarrier, double-buffered so the
+//    next tile streams in while this one computes; out-of-range rows/columns
+//    are zero-filled by TMA and never read (clamp maps inside the grid);
+//  * each thread owns one column of 8 rows with a sliding vertical window
+//    (3 shared loads per point), interior tiles skip all clamp arithmetic;
+//  * every mbarrier wait is bounded: on timeout the kernel raises an error bit
+//    and returns instead of hanging.
+// `iterate` runs as a captured CUDA graph of the step launches (ping-pong
+// buffers, one tensor map per buffer), cached per (kind, shape, buffers,
+// steps).  Shapes TMA cannot describe (odd width, misaligned base) use a
+// plain clamped kernel with the same arithmetic.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "hyd_common.cuh"
+
+namespace hyd {
+
+enum { ST_LAPLACIAN = 0, ST_JACOBI = 1, ST_HEAT = 2, ST_HEAT_EXAMPLE = 3 };
+
+template <int KIND>
+__device__ __forceinline__ double stencil_body(double a, double b, double c, double d, double e) {
+    const double t3 = __dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d);
+    if (KIND == ST_LAPLACIAN) return __fma_rn(e, -4.0, t3);
+    if (KIND == ST_JACOBI) return __dmul_rn(t3, 0.25);
+    if (KIND == ST_HEAT) {
+        const double lap = __fma_rn(-4.0, e, t3);
+        return __dadd_rn(e, __dmul_rn(0.1, lap));
+    }
+    return __ddiv_rn(__dadd_rn(t3, e), 5.0);
+}
+
+// ---------------------------------------------------------------- plain path
+template <int KIND>
+__global__ void __launch_bounds__(256) stencil_plain_kernel(const double* __restrict__ in,
+                                                            double* __restrict__ out, int64_t h,
+                                                            int64_t w) {
+    const int64_t j = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
+    const int64_t i = (int64_t)blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (i >= h || j >= w) return;
+    const int64_t im = i > 0 ? i - 1 : 0, ip = i + 1 < h ? i + 1 : h - 1;
+    const int64_t jm = j > 0 ? j - 1 : 0, jp = j + 1 < w ? j + 1 : w - 1;
+    out[i * w + j] = stencil_body<KIND>(in[im * w + j], in[ip * w + j], in[i * w + jm],
+                                        in[i * w + jp], in[i * w + j]);
+}
+
+// ---------------------------------------------------------------- TMA path
+constexpr int kTH = 16;                 // output rows per tile
+constexpr int kTW = 128;                // output columns per tile
+constexpr int kBoxW = kTW + 4;          // input box columns (2-column halo each side)
+constexpr int kBoxH = kTH + 2;          // input box rows
+constexpr int kStThreads = 256;
+constexpr int kRowsPerThread = kTH * kTW / kStThreads;  // 8
+constexpr int kStageBytes = kBoxW * kBoxH * 8;          // 19008
+constexpr int kStageStride = (kStageBytes + 1023) & ~1023;
+constexpr unsigned kTmaWaitLimit = 1u << 22;            // polls before a wait gives up
+
+__device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned addr, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test_wait(unsigned addr, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait (non-blocking polls with a short sleep between them, about a
+// quarter of a second in total); false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity) {
+    for (unsigned it = 0; it < kTmaWaitLimit; ++it) {
+        if (mbar_test_wait(addr, parity)) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap* map, int x, int y,
+                                            unsigned mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kStThreads)
+    stencil_tma_kernel(const __grid_constant__ CUtensorMap in_map, double* __restrict__ out,
+                       int h, int w, unsigned* err) {
+    extern __shared__ __align__(1024) unsigned char sm_raw[];
+    // stages at 1024-byte aligned offsets, barriers after them
+    unsigned char* base = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(sm_raw) + 1023) & ~uintptr_t(1023));
+    // stage s at base + s*kStageStride, its barrier at bars + 8*s
+    const unsigned stage0 = (unsigned)__cvta_generic_to_shared(base);
+    const unsigned bar0 = stage0 + 2 * kStageStride;
+    const int ntj = (w + kTW - 1) / kTW;
+    const int nti = (h + kTH - 1) / kTH;
+    const int ntiles = nti * ntj;
+    if (threadIdx.x == 0) {
+        mbar_init(bar0, 1);
+        mbar_init(bar0 + 8, 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+
+    int tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < ntiles) {
+        mbar_expect_tx(bar0, kStageBytes);
+        tma_load_2d(stage0, &in_map, (tile % ntj) * kTW - 2, (tile / ntj) * kTH - 1, bar0);
+    }
+    const int col = threadIdx.x % kTW;
+    const int rgrp = threadIdx.x / kTW;  // 0..1: rows rgrp*8 .. rgrp*8+7
+    bool timed_out = false;
+    int it = 0;
+    for (; tile < ntiles; ++it, tile += gridDim.x) {
+        const int s = it & 1;
+        const unsigned parity = (unsigned)(it >> 1) & 1u;  // use count of stage s, mod 2
+        const int next = tile + gridDim.x;
+        if (threadIdx.x == 0 && next < ntiles) {
+            const unsigned so = (unsigned)(s ^ 1);
+            mbar_expect_tx(bar0 + 8 * so, kStageBytes);
+            tma_load_2d(stage0 + so * kStageStride, &in_map, (next % ntj) * kTW - 2, (next / ntj) * kTH - 1,
+                        bar0 + 8 * so);
+        }
+        const bool ok = mbar_wait_bounded(bar0 + 8 * (unsigned)s, parity);
+        if (__syncthreads_or(!ok)) {  // block-uniform decision
+            timed_out = true;
+            break;
+        }
+        const double* sm = reinterpret_cast<const double*>(base + s * kStageStride);
+        const int i0 = (tile / ntj) * kTH, j0 = (tile % ntj) * kTW;
+        const int j = j0 + col;
+        const bool interior = i0 >= 1 && i0 + kTH + 1 <= h && j0 >= 1 && j0 + kTW + 1 <= w;
+        const int r0 = rgrp * kRowsPerThread;
+        if (interior) {
+            // smem row r <-> global row i0 - 1 + r; smem col c <-> global col j0 - 2 + c
+            const int c = col + 2;
+            double up = sm[(r0) * kBoxW + c];
+            double mid = sm[(r0 + 1) * kBoxW + c];
+            double* o = out + (int64_t)(i0 + r0) * w + j;
+#pragma unroll
+            for (int k = 0; k < kRowsPerThread; ++k) {
+                const int r = r0 + 1 + k;
+                const double dn = sm[(r + 1) * kBoxW + c];
+                const double lf = sm[r * kBoxW + c - 1];
+                const double rt = sm[r * kBoxW + c + 1];
+                o[(int64_t)k * w] = stencil_body<KIND>(up, dn, lf, rt, mid);
+                up = mid;
+                mid = dn;
+            }
+        } else if (j < w) {
+            const int jm = (j > 0 ? j - 1 : 0) - j0 + 2, jp = (j + 1 < w ? j + 1 : w - 1) - j0 + 2;
+            const int jc = col + 2;
+#pragma unroll
+            for (int k = 0; k < kRowsPerThread; ++k) {
+                const int i = i0 + r0 + k;
+                if (i < h) {
+                    const int im = (i > 0 ? i - 1 : 0) - i0 + 1, ip = (i + 1 < h ? i + 1 : h - 1) - i0 + 1;
+                    const int ic = i - i0 + 1;
+                    out[(int64_t)i * w + j] = stencil_body<KIND>(sm[im * kBoxW + jc], sm[ip * kBoxW + jc],
+                                                                 sm[ic * kBoxW + jm], sm[ic * kBoxW + jp],
+                                                                 sm[ic * kBoxW + jc]);
+                }
+            }
+        }
+        __syncthreads();  // stage s fully read before it is refilled next iteration
+    }
+    if (timed_out) {
+        if (threadIdx.x == 0) raise_error(err, ERRBIT_TIMEOUT);
+        // wait (bounded) for the copies that may still land in this CTA's
+        // stages: the stage being waited on and the one prefetched after it
+        mbar_wait_bounded(bar0 + 8 * (unsigned)(it & 1), (unsigned)(it >> 1) & 1u);
+        if (tile + (int)gridDim.x < ntiles)
+            mbar_wait_bounded(bar0 + 8 * (unsigned)((it + 1) & 1), (unsigned)((it + 1) >> 1) & 1u);
+    }
+}
+
+constexpr size_t kTmaSmem = 2 * kStageStride + 64 + 1024;
+
+// --- driver entry point for tensor-map encoding --------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+static bool tma_ok(const double* p, int64_t h, int64_t w) {
+    return encode_fn() != nullptr && (reinterpret_cast<uintptr_t>(p) & 15) == 0 && (w % 2) == 0 &&
+           w >= 2 && h >= 1 && w <= (1LL << 31) - 1 && h <= (1LL << 31) - 1;
+}
+
+static int make_map(CUtensorMap* map, const double* p, int64_t h, int64_t w) {
+    cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)h};
+    cuuint64_t strides[1] = {(cuuint64_t)w * 8};
+    cuuint32_t box[2] = {(cuuint32_t)kBoxW, (cuuint32_t)kBoxH};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(p), dims, strides, box,
+                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(HYD_CUDA_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return HYD_CUDA_OK;
+}
+
+template <int KIND>
+static int launch_step_kind(const CUtensorMap* map, const double* in, double* out, int64_t h, int64_t w,
+                            bool tma, const Device* d, cudaStream_t stream) {
+    if (tma) {
+        auto k = stencil_tma_kernel<KIND>;
+        HYD_TRY(configure_kernel((const void*)k, d, false));
+        const int64_t ntiles = ((h + kTH - 1) / kTH) * ((w + kTW - 1) / kTW);
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kStThreads, kTmaSmem);
+        if (occ < 1) occ = 1;
+        int64_t grid = (int64_t)d->sm_count * occ;
+        if (grid > ntiles) grid = ntiles;
+        k<<<(unsigned)grid, kStThreads, kTmaSmem, stream>>>(*map, out, (int)h, (int)w, d->d_err);
+    } else {
+        dim3 grid((unsigned)((w + 31) / 32), (unsigned)((h + 7) / 8));
+        stencil_plain_kernel<KIND><<<grid, 256, 0, stream>>>(in, out, h, w);
+    }
+    return launch_check("stencil2d_f64");
+}
+
+static int launch_step(int kind, const CUtensorMap* map, const double* in, double* out, int64_t h, int64_t w,
+                       bool tma, const Device* d, cudaStream_t stream) {
+    switch (kind) {
+        case ST_LAPLACIAN: return launch_step_kind<ST_LAPLACIAN>(map, in, out, h, w, tma, d, stream);
+        case ST_JACOBI: return launch_step_kind<ST_JACOBI>(map, in, out, h, w, tma, d, stream);
+        case ST_HEAT: return launch_step_kind<ST_HEAT>(map, in, out, h, w, tma, d, stream);
+        default: return launch_step_kind<ST_HEAT_EXAMPLE>(map, in, out, h, w, tma, d, stream);
+    }
+}
+
+// Cached executable graphs of whole `iterate` runs.
+struct GraphKey {
+    int kind;
+    int64_t h, w, iters;
+    const void *b0, *b1;
+    cudaStream_t stream;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(kind, h, w, iters, b0, b1, stream) < std::tie(o.kind, o.h, o.w, o.iters, o.b0, o.b1, o.stream);
+    }
+};
+static std::mutex g_graph_mu;
+static std::map<GraphKey, cudaGraphExec_t> g_graphs;
+
+}  // namespace hyd
+
+using namespace hyd;
+
+extern "C" int hyd_cuda_stencil2d_f64(int kind, const double* in, double* out, int64_t h, int64_t w,
+                                      void* stream) {
+    HYD_CHECK_ARG(kind >= 0 && kind <= 3, "stencil2d: unknown kind %d", kind);
+    HYD_CHECK_ARG(h >= 0 && w >= 0, "stencil2d: negative shape");
+    HYD_CHECK_ARG(h * w == 0 || (in != nullptr && out != nullptr), "stencil2d: null buffer");
+    HYD_CHECK_ARG(in != out || h * w == 0, "stencil2d: input and output must differ");
+    if (h == 0 || w == 0) return HYD_CUDA_OK;
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    const bool tma = tma_ok(in, h, w);
+    CUtensorMap map;
+    if (tma) HYD_TRY(make_map(&map, in, h, w));
+    return launch_step(kind, &map, in, out, h, w, tma, d, as_stream(stream));
+}
+
+extern "C" int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
+                                              int64_t iters, int* final_buf, void* stream) {
+    HYD_CHECK_ARG(kind >= 0 && kind <= 3, "iterate_stencil2d: unknown kind %d", kind);
+    HYD_CHECK_ARG(h >= 0 && w >= 0 && iters >= 0, "iterate_stencil2d: negative shape or count");
+    HYD_CHECK_ARG(final_buf != nullptr, "iterate_stencil2d: null final_buf");
+    HYD_CHECK_ARG(h * w == 0 || (buf0 != nullptr && buf1 != nullptr && buf0 != buf1),
+                  "iterate_stencil2d: need two distinct buffers");
+    *final_buf = (int)(iters & 1);
+    if (h == 0 || w == 0 || iters == 0) return HYD_CUDA_OK;
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    cudaStream_t st = as_stream(stream);
+    const bool tma = tma_ok(buf0, h, w) && tma_ok(buf1, h, w);
+    CUtensorMap maps[2];
+    if (tma) {
+        HYD_TRY(make_map(&maps[0], buf0, h, w));
+        HYD_TRY(make_map(&maps[1], buf1, h, w));
+    }
+    double* bufs[2] = {buf0, buf1};
+    // Graph capture needs a non-default stream; on the legacy stream run eagerly.
+    if (st == nullptr || iters < 4) {
+        for (int64_t t = 0; t < iters; ++t)
+            HYD_TRY(launch_step(kind, &maps[t & 1], bufs[t & 1], bufs[(t + 1) & 1], h, w, tma, d, st));
+        return HYD_CUDA_OK;
+    }
+    GraphKey key{kind, h, w, iters, buf0, buf1, st};
+    cudaGraphExec_t exec = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_graph_mu);
+        auto it = g_graphs.find(key);
+        if (it != g_graphs.end()) exec = it->second;
+    }
+    if (!exec) {
+        // warm the per-kernel configuration outside capture
+        HYD_TRY(launch_step(kind, &maps[0], bufs[0], bufs[1], h, w, tma, d, st));
+        HYD_CUDA_TRY(cudaStreamSynchronize(st));
+        cudaGraph_t graph = nullptr;
+        HYD_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int status = HYD_CUDA_OK;
+        for (int64_t t = 0; t < iters && status == HYD_CUDA_OK; ++t)
+            status = launch_step(kind, &maps[t & 1], bufs[t & 1], bufs[(t + 1) & 1], h, w, tma, d, st);
+        cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (status != HYD_CUDA_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return status;
+        }
+        HYD_CUDA_TRY(ce);
+        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        HYD_CUDA_TRY(ie);
+        std::lock_guard<std::mutex> lock(g_graph_mu);
+        g_graphs[key] = exec;
+    }
+    HYD_CUDA_TRY(cudaGraphLaunch(exec, st));
+    return HYD_CUDA_OK;
+}
+
+extern "C" void hyd_cuda_stencil_release_graphs(void) {
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
+    g_graphs.clear();
+}

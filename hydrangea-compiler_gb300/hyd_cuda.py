@@ -18,6 +18,7 @@ OK = 0
 ERR_INVALID, ERR_NOMEM, ERR_CUDA, ERR_NO_DEVICE, ERR_BOUNDS = 1, 2, 3, 4, 5
 ERR_TIMEOUT, ERR_BUDGET, ERR_CANCELLED, ERR_UNSUPPORTED = 6, 7, 8, 9
 
+STENCIL_LAPLACIAN, STENCIL_JACOBI, STENCIL_HEAT, STENCIL_HEAT_EXAMPLE = 0, 1, 2, 3
 SCATTER_AUTO, SCATTER_SMEM_WARP, SCATTER_SMEM_BLOCK, SCATTER_CLUSTER, SCATTER_GLOBAL = 0, 1, 2, 3, 4
 
 _p = C.c_void_p
@@ -44,6 +45,9 @@ SIGNATURES = {
     "hyd_cuda_weighted_histogram_i64": (_i, [_p, _i64, _i64, _p, _i, _p]),
     "hyd_cuda_scatter_add_i64": (_i, [_p, _p, _i64, _p, _i64, _i, _p]),
     "hyd_cuda_scatter_add_f64": (_i, [_p, _p, _i64, _p, _i64, _p]),
+    "hyd_cuda_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _p]),
+    "hyd_cuda_iterate_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _i64, C.POINTER(C.c_int), _p]),
+    "hyd_cuda_stencil_release_graphs": (None, []),
     "hyd_cuda_weighted_histogram_host": (_i, [_p, _i64, _i64, _p, _i]),
     "hyd_cuda_dot_f64_host": (_i, [_p, _p, _i64, _p]),
     "hyd_cuda_array_alloc": (_p, [None, C.c_size_t]),
@@ -166,6 +170,20 @@ def scatter_add_i64(idx, vals, dst, strategy=SCATTER_AUTO, stream=None):
 def scatter_add_f64(idx, vals, dst, stream=None):
     call("hyd_cuda_scatter_add_f64", ptr(idx), ptr(vals), idx.numel(), ptr(dst), dst.numel(),
          stream_handle(stream))
+
+
+def stencil2d(kind, src, dst, stream=None):
+    h, w = src.shape
+    call("hyd_cuda_stencil2d_f64", kind, ptr(src), ptr(dst), h, w, stream_handle(stream))
+
+
+def iterate_stencil2d(kind, buf0, buf1, iters, stream=None):
+    """Runs `iters` steps ping-ponging buf0/buf1; returns the buffer holding the result."""
+    h, w = buf0.shape
+    fb = C.c_int(-1)
+    call("hyd_cuda_iterate_stencil2d_f64", kind, ptr(buf0), ptr(buf1), h, w, iters, C.byref(fb),
+         stream_handle(stream))
+    return buf0 if fb.value == 0 else buf1
 
 
 def make_array(np_array):

@@ -133,6 +133,33 @@ int hyd_cuda_scatter_add_i64(const int64_t* idx, const int64_t* vals, int64_t n,
 int hyd_cuda_scatter_add_f64(const int64_t* idx, const double* vals, int64_t n,
                              double* dst, int64_t dst_n, void* stream);
 
+/* ---- 2-D clamp stencils and iterate ---------------------------------------
+ * Replaces the split-region clamp stencil loops (Lowering.hs:1932-2035,
+ * :2562-2661; each region an `omp parallel for`) and the ping-pong iterate
+ * (Lowering.hs:840-858, CFGOpt.hs:795-810).  5-point footprint, clamp-to-edge,
+ * row-major float64 [h][w].  Bodies, evaluated left to right as the program
+ * text (a = acc (-1) 0, b = acc 1 0, c = acc 0 (-1), d = acc 0 1, e = acc 0 0):
+ *   HYD_STENCIL_LAPLACIAN     a + b + c + d + (e * -4.0)    bench/stencil/stencil_2d.hyd
+ *   HYD_STENCIL_JACOBI        (a + b + c + d) / 4.0          bench/stencil/jacobi_2d.hyd
+ *   HYD_STENCIL_HEAT          e + 0.1 * (a+b+c+d - 4.0*e)    heat step of the 8192^2 workload
+ *   HYD_STENCIL_HEAT_EXAMPLE  (a + b + c + d + e) / 5.0      examples/heat_2d.hyd
+ * Results are bit-identical to the C backend. */
+typedef enum {
+    HYD_STENCIL_LAPLACIAN = 0,
+    HYD_STENCIL_JACOBI = 1,
+    HYD_STENCIL_HEAT = 2,
+    HYD_STENCIL_HEAT_EXAMPLE = 3
+} hyd_stencil_kind_t;
+int hyd_cuda_stencil2d_f64(int kind, const double* in, double* out, int64_t h, int64_t w, void* stream);
+/* iterate iters (stencil kind) over buf0 with ping-pong into buf1; *final_buf
+ * is set to the buffer (0 or 1) holding the result.  On a non-default stream
+ * the whole run is a captured CUDA graph, cached per (kind, shape, buffers,
+ * iters, stream) and replayed on later calls. */
+int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
+                                   int64_t iters, int* final_buf, void* stream);
+/* Releases the cached iterate graphs (also done by hyd_cuda_cleanup). */
+void hyd_cuda_stencil_release_graphs(void);
+
 /* ---- host-memory entry points (embedding boundary) --------------------------
  * Same computations on HOST pointers: the input is streamed to the device in
  * 64 MiB chunks on two streams (copy of chunk k+1 overlaps the kernel on chunk
