@@ -48,6 +48,15 @@ SIGNATURES = {
     "hyd_cuda_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _p]),
     "hyd_cuda_iterate_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _i64, C.POINTER(C.c_int), _p]),
     "hyd_cuda_stencil_release_graphs": (None, []),
+    "hyd_cuda_scan_i64": (_i, [_p, _p, _i64, _i64, _i, _i, _p]),
+    "hyd_cuda_scan_f64": (_i, [_p, _p, _i64, _d, _i, _i, _p]),
+    "hyd_cuda_segmented_reduce_i64": (_i, [_p, _i64, _p, _i64, _i64, _p, _p]),
+    "hyd_cuda_segmented_reduce_f64": (_i, [_p, _i64, _p, _i64, _d, _p, _p]),
+    "hyd_cuda_sort_indices_i64": (_i, [_p, _i64, _p, _p]),
+    "hyd_cuda_sort_indices_bits_i64": (_i, [_p, _i64, _i, _p, _p]),
+    "hyd_cuda_gather_i64": (_i, [_p, _i64, _p, _i64, _p, _p]),
+    "hyd_cuda_gather_f64": (_i, [_p, _i64, _p, _i64, _p, _p]),
+    "hyd_cuda_gather_i32": (_i, [_p, _i64, _p, _i64, _p, _p]),
     "hyd_cuda_weighted_histogram_host": (_i, [_p, _i64, _i64, _p, _i]),
     "hyd_cuda_dot_f64_host": (_i, [_p, _p, _i64, _p]),
     "hyd_cuda_array_alloc": (_p, [None, C.c_size_t]),
@@ -184,6 +193,33 @@ def iterate_stencil2d(kind, buf0, buf1, iters, stream=None):
     call("hyd_cuda_iterate_stencil2d_f64", kind, ptr(buf0), ptr(buf1), h, w, iters, C.byref(fb),
          stream_handle(stream))
     return buf0 if fb.value == 0 else buf1
+
+
+def scan(x, out, init=0, reverse=False, inclusive=False, stream=None):
+    import torch
+    fn = "hyd_cuda_scan_i64" if x.dtype == torch.int64 else "hyd_cuda_scan_f64"
+    call(fn, ptr(x), ptr(out), x.numel(), init, int(reverse), int(inclusive), stream_handle(stream))
+
+
+def segmented_reduce(offsets, vals, out, init=0, stream=None):
+    import torch
+    fn = "hyd_cuda_segmented_reduce_i64" if vals.dtype == torch.int64 else "hyd_cuda_segmented_reduce_f64"
+    call(fn, ptr(offsets), offsets.numel(), ptr(vals), vals.numel(), init, ptr(out), stream_handle(stream))
+
+
+def sort_indices(keys, perm, key_bits=None, stream=None):
+    if key_bits is None:
+        call("hyd_cuda_sort_indices_i64", ptr(keys), keys.numel(), ptr(perm), stream_handle(stream))
+    else:
+        call("hyd_cuda_sort_indices_bits_i64", ptr(keys), keys.numel(), key_bits, ptr(perm),
+             stream_handle(stream))
+
+
+def gather(perm, src, out, stream=None):
+    import torch
+    fn = {torch.int64: "hyd_cuda_gather_i64", torch.float64: "hyd_cuda_gather_f64",
+          torch.int32: "hyd_cuda_gather_i32"}[src.dtype]
+    call(fn, ptr(perm), perm.numel(), ptr(src), src.numel(), ptr(out), stream_handle(stream))
 
 
 def make_array(np_array):

@@ -160,6 +160,47 @@ int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t
 /* Releases the cached iterate graphs (also done by hyd_cuda_cleanup). */
 void hyd_cuda_stencil_release_graphs(void);
 
+/* ---- scan family and segmented reduce ----------------------------------------
+ * scan / scan_inclusive / scanr / scanr_inclusive with (+) and initial value
+ * `init` (Lowering.hs:3563-3612; the reference runs them as a serial fold):
+ * reverse != 0 walks index n-1-k; inclusive != 0 writes the accumulator after
+ * adding element k, otherwise before.  int64: single-pass decoupled look-back,
+ * bit-exact.  float64: deterministic reduce-then-scan (three launches); within
+ * 1e-12 of the prefix sums of |x| of the serial fold. */
+int hyd_cuda_scan_i64(const int64_t* in, int64_t* out, int64_t n, int64_t init, int reverse,
+                      int inclusive, void* stream);
+int hyd_cuda_scan_f64(const double* in, double* out, int64_t n, double init, int reverse,
+                      int inclusive, void* stream);
+/* segmented_reduce (+) init offsets vals (Lowering.hs:874-944): out[s] = init +
+ * sum of vals[offsets[s] .. offsets[s+1]).  n_offsets = segments + 1.  A
+ * segment outside [0, n_vals] or with decreasing offsets yields init and is
+ * reported by hyd_cuda_check.  int64 bit-exact; float64 deterministic, within
+ * 1e-12 of the sum of |vals| of the segment. */
+int hyd_cuda_segmented_reduce_i64(const int64_t* offsets, int64_t n_offsets, const int64_t* vals,
+                                  int64_t n_vals, int64_t init, int64_t* out, void* stream);
+int hyd_cuda_segmented_reduce_f64(const int64_t* offsets, int64_t n_offsets, const double* vals,
+                                  int64_t n_vals, double init, double* out, void* stream);
+
+/* ---- sort_indices and gather ---------------------------------------------------
+ * sort_indices keys (runtime/hydrangea_runtime.h:386-456): the permutation
+ * that stably sorts `keys` by the runtime's LSD radix digits ((key >> 8p) &
+ * 0xFF on the signed key, passes = bytes of max(0, max key), at least one), so
+ * the permutation is identical to the reference runtime's.  perm is int64.
+ * hyd_cuda_sort_indices_i64 finds the pass count on the device (one 8-byte
+ * read-back); the _bits variant takes it from the caller (keys known to fit in
+ * key_bits bits; same result when that bound holds). */
+int hyd_cuda_sort_indices_i64(const int64_t* keys, int64_t n, int64_t* perm, void* stream);
+int hyd_cuda_sort_indices_bits_i64(const int64_t* keys, int64_t n, int key_bits, int64_t* perm,
+                                   void* stream);
+/* gather perm src: out[i] = src[perm[i]]; an index outside [0, src_n) leaves
+ * out[i] unwritten and is reported by hyd_cuda_check. */
+int hyd_cuda_gather_i64(const int64_t* perm, int64_t n, const int64_t* src, int64_t src_n,
+                        int64_t* out, void* stream);
+int hyd_cuda_gather_f64(const int64_t* perm, int64_t n, const double* src, int64_t src_n,
+                        double* out, void* stream);
+int hyd_cuda_gather_i32(const int64_t* perm, int64_t n, const int32_t* src, int64_t src_n,
+                        int32_t* out, void* stream);
+
 /* ---- host-memory entry points (embedding boundary) --------------------------
  * Same computations on HOST pointers: the input is streamed to the device in
  * 64 MiB chunks on two streams (copy of chunk k+1 overlaps the kernel on chunk
