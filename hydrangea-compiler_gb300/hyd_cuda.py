@@ -57,6 +57,12 @@ SIGNATURES = {
     "hyd_cuda_gather_i64": (_i, [_p, _i64, _p, _i64, _p, _p]),
     "hyd_cuda_gather_f64": (_i, [_p, _i64, _p, _i64, _p, _p]),
     "hyd_cuda_gather_i32": (_i, [_p, _i64, _p, _i64, _p, _p]),
+    "hyd_cuda_coo_sum_duplicates_i64": (_i, [_p, _p, _p, _i64, _p, _p, _p, _p, _p]),
+    "hyd_cuda_csr_from_sorted_coo_i64": (_i, [_i64, _i64, _p, _p, _p, _p, _p, _p, _p]),
+    "hyd_cuda_spmv_csr_f64": (_i, [_i64, _i64, _p, _p, _p, _p, _p, _i, _p]),
+    "hyd_cuda_spmv_csr_i32_f64": (_i, [_i64, _i64, _p, _p, _p, _p, _p, _i, _p]),
+    "hyd_cuda_batched_coo_csr_spmv_f64": (_i, [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
+    "hyd_cuda_synth_coo_batch": (_i, [_i64, _u64, _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p]),
     "hyd_cuda_weighted_histogram_host": (_i, [_p, _i64, _i64, _p, _i]),
     "hyd_cuda_dot_f64_host": (_i, [_p, _p, _i64, _p]),
     "hyd_cuda_array_alloc": (_p, [None, C.c_size_t]),
@@ -220,6 +226,69 @@ def gather(perm, src, out, stream=None):
     fn = {torch.int64: "hyd_cuda_gather_i64", torch.float64: "hyd_cuda_gather_f64",
           torch.int32: "hyd_cuda_gather_i32"}[src.dtype]
     call(fn, ptr(perm), perm.numel(), ptr(src), src.numel(), ptr(out), stream_handle(stream))
+
+
+def coo_sum_duplicates(rows, cols, vals, stream=None):
+    import torch
+    n = rows.numel()
+    o_r, o_c, o_v = (torch.empty_like(rows) for _ in range(3))
+    k = torch.zeros(1, dtype=torch.int64, device=rows.device)
+    call("hyd_cuda_coo_sum_duplicates_i64", ptr(rows), ptr(cols), ptr(vals), n, ptr(o_r), ptr(o_c), ptr(o_v),
+         ptr(k), stream_handle(stream))
+    return o_r, o_c, o_v, k
+
+
+def csr_from_sorted_coo(nrows, nnz, rows, cols, vals, stream=None):
+    import torch
+    row_ptr = torch.zeros(nrows + 1, dtype=torch.int64, device=rows.device)
+    col_idx = torch.zeros_like(cols)
+    out_vals = torch.zeros_like(vals)
+    call("hyd_cuda_csr_from_sorted_coo_i64", nrows, nnz, ptr(rows), ptr(cols), ptr(vals), ptr(row_ptr),
+         ptr(col_idx), ptr(out_vals), stream_handle(stream))
+    return row_ptr, col_idx, out_vals
+
+
+def spmv_csr(row_ptr, col_idx, vals, x, y, lanes_per_row=0, stream=None):
+    import torch
+    fn = "hyd_cuda_spmv_csr_f64" if col_idx.dtype == torch.int64 else "hyd_cuda_spmv_csr_i32_f64"
+    call(fn, row_ptr.numel() - 1, x.numel(), ptr(row_ptr), ptr(col_idx), ptr(vals), ptr(x), ptr(y),
+         lanes_per_row, stream_handle(stream))
+
+
+def synth_coo_batch(ninst, seed0=4, min_log2=10, max_log2=18, max_row_len=256, device="cuda", stream=None):
+    """Allocates and fills a synthetic batch; returns (desc ndarray, rows, cols, vals, x)."""
+    import numpy as np
+    import torch
+    desc = np.zeros((ninst, 3), dtype=np.int64)
+    call("hyd_cuda_synth_coo_batch", ninst, seed0, min_log2, max_log2, max_row_len, desc.ctypes.data,
+         None, None, None, None, 0, stream_handle(stream))
+    nnz = int(desc[:, 2].sum())
+    nx = int(desc[:, 1].sum())
+    rows = torch.empty(max(nnz, 1), dtype=torch.int32, device=device)
+    cols = torch.empty(max(nnz, 1), dtype=torch.int32, device=device)
+    vals = torch.empty(max(nnz, 1), dtype=torch.float64, device=device)
+    x = torch.empty(nx, dtype=torch.float64, device=device)
+    call("hyd_cuda_synth_coo_batch", ninst, seed0, min_log2, max_log2, max_row_len, desc.ctypes.data,
+         ptr(rows), ptr(cols), ptr(vals), ptr(x), rows.numel(), stream_handle(stream))
+    return desc, rows, cols, vals, x
+
+
+def batched_coo_csr_spmv(desc, rows, cols, vals, x, stream=None):
+    """Returns (row_ptr, csr_cols, csr_vals, y) for a concatenated batch."""
+    import numpy as np
+    import torch
+    desc = np.ascontiguousarray(desc, dtype=np.int64)
+    ninst = desc.shape[0]
+    nnz = int(desc[:, 2].sum())
+    nr = int(desc[:, 0].sum())
+    dev = x.device
+    row_ptr = torch.zeros(nr + ninst, dtype=torch.int64, device=dev)
+    csr_cols = torch.zeros(max(nnz, 1), dtype=torch.int32, device=dev)
+    csr_vals = torch.zeros(max(nnz, 1), dtype=torch.float64, device=dev)
+    y = torch.zeros(nr, dtype=torch.float64, device=dev)
+    call("hyd_cuda_batched_coo_csr_spmv_f64", ninst, desc.ctypes.data, ptr(rows), ptr(cols), ptr(vals), ptr(x),
+         ptr(row_ptr), ptr(csr_cols), ptr(csr_vals), ptr(y), stream_handle(stream))
+    return row_ptr, csr_cols, csr_vals, y
 
 
 def make_array(np_array):

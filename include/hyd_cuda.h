@@ -201,6 +201,54 @@ int hyd_cuda_gather_f64(const int64_t* perm, int64_t n, const double* src, int64
 int hyd_cuda_gather_i32(const int64_t* perm, int64_t n, const int32_t* src, int64_t src_n,
                         int32_t* out, void* stream);
 
+/* ---- COO / CSR / SpMV ------------------------------------------------------------
+ * coo_sum_duplicates (Lowering.hs:966-1080): merges adjacent entries with equal
+ * (row, col) of a sorted COO, summing their int64 values.  Outputs have the
+ * input's length; entries past the canonical count are zero, as in the
+ * reference's calloc'd result.  *out_nnz (device int64) receives the count. */
+int hyd_cuda_coo_sum_duplicates_i64(const int64_t* rows, const int64_t* cols, const int64_t* vals,
+                                    int64_t nnz, int64_t* out_rows, int64_t* out_cols,
+                                    int64_t* out_vals, int64_t* out_nnz, void* stream);
+/* csr_from_sorted_coo (Lowering.hs:1081-1160): row_ptr[nrows+1] = exclusive
+ * running sum of per-row counts (total last), col_idx/out_vals = the first
+ * nnz cols/vals copied through.  A row outside [0, nrows) is reported by
+ * hyd_cuda_check. */
+int hyd_cuda_csr_from_sorted_coo_i64(int64_t nrows, int64_t nnz, const int64_t* rows,
+                                     const int64_t* cols, const int64_t* vals, int64_t* row_ptr,
+                                     int64_t* col_idx, int64_t* out_vals, void* stream);
+/* SpMV y = A x over CSR (bench/spmv/spmv.hyd:30-40): lanes_per_row lanes (power
+ * of two <= 32, 0 = default 8) share a row with fma partial sums and a fixed
+ * xor tree: deterministic, within 1e-12 of sum |v*x| of the sequential C sum.
+ * A column outside [0, ncols) is skipped and reported. */
+int hyd_cuda_spmv_csr_f64(int64_t nrows, int64_t ncols, const int64_t* row_ptr, const int64_t* col_idx,
+                          const double* vals, const double* x, double* y, int lanes_per_row, void* stream);
+int hyd_cuda_spmv_csr_i32_f64(int64_t nrows, int64_t ncols, const int64_t* row_ptr,
+                              const int32_t* col_idx, const double* vals, const double* x, double* y,
+                              int lanes_per_row, void* stream);
+/* Batched COO -> CSR -> SpMV over ninst instances in one persistent pass.
+ * desc: HOST array of ninst x (nrows, ncols, nnz).  Device arrays are the
+ * instances concatenated in order: rows/cols (int32, device narrowing of the
+ * int64 ABI, valid for extents < 2^31), vals, csr_cols, csr_vals by entries;
+ * x by ncols; y by nrows; row_ptr by nrows + 1 (each instance's row_ptr starts
+ * at 0).  Per instance the CSR equals sorting the entries by (row, col) (the
+ * packed-key pipeline of bench/coo_csr_build/coo_csr_build.hyd:37-62) and y is
+ * its SpMV.  Contract: no duplicate (row, col) in an instance, at most 256
+ * entries per row (the workload's cap); a longer row or an out-of-range entry is
+ * reported by hyd_cuda_check.  Synchronizes the stream before returning. */
+int hyd_cuda_batched_coo_csr_spmv_f64(int64_t ninst, const int64_t* desc, const int32_t* rows,
+                                      const int32_t* cols, const double* vals, const double* x,
+                                      int64_t* row_ptr, int32_t* csr_cols, double* csr_vals, double* y,
+                                      void* stream);
+/* Seeded synthetic batch: ninst square instances, instance i from seed seed0+i
+ * with n = floor(2^(min_log2 + (max_log2-min_log2) u)), rows of Zipf(1.5)
+ * length on {1..max_row_len}, distinct columns, values and x uniform in
+ * [-1, 1), entries stored in a shuffled order.  Always fills desc (HOST,
+ * ninst x 3); when rows is NULL only the sizes are computed, otherwise
+ * rows/cols/vals (capacity_entries) and x (sum of n) are filled. */
+int hyd_cuda_synth_coo_batch(int64_t ninst, uint64_t seed0, int min_log2, int max_log2, int max_row_len,
+                             int64_t* desc, int32_t* rows, int32_t* cols, double* vals, double* x,
+                             int64_t capacity_entries, void* stream);
+
 /* ---- host-memory entry points (embedding boundary) --------------------------
  * Same computations on HOST pointers: the input is streamed to the device in
  * 64 MiB chunks on two streams (copy of chunk k+1 overlaps the kernel on chunk
