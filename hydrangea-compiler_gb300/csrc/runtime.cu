@@ -118,7 +118,11 @@ int configure_kernel(const void* fn, const Device* d, bool nonportable_cluster) 
     unsigned& mask = done[fn];
     const unsigned bit = 1u << (d->id & 31);
     if (mask & bit) return HYD_CUDA_OK;
-    HYD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d->max_smem_optin));
+    // dynamic + static shared memory may not exceed the opt-in maximum
+    cudaFuncAttributes fa;
+    HYD_CUDA_TRY(cudaFuncGetAttributes(&fa, fn));
+    HYD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      d->max_smem_optin - (int)fa.sharedSizeBytes));
     if (nonportable_cluster)
         HYD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     mask |= bit;

@@ -33,6 +33,7 @@
 #include <cstring>
 #include <vector>
 
+#include "batch.cuh"
 #include "hyd_common.cuh"
 
 namespace hyd {
@@ -94,19 +95,27 @@ __global__ void __launch_bounds__(256) spmv_csr_kernel(int64_t nrows, const long
                                                        const double* __restrict__ x, int64_t ncols,
                                                        double* __restrict__ y, unsigned* err) {
     const int sub = threadIdx.x & (G - 1);
-    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+    constexpr int kRowsPerWarp = 32 / G;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int group = (threadIdx.x & 31) / G;
     bool bad = false;
-    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < nrows; r += groups) {
-        const long long s = row_ptr[r], e = row_ptr[r + 1];
+    // warp-uniform loop: every lane of a warp runs the same iterations, so the
+    // full-mask shuffles below always see all 32 lanes
+    for (int64_t rb = warp * kRowsPerWarp; rb < nrows; rb += warps * kRowsPerWarp) {
+        const int64_t r = rb + group;
         double acc = 0.0;
-        for (long long k = s + sub; k < e; k += G) {
-            const long long c = (long long)col_idx[k];
-            if ((unsigned long long)c < (unsigned long long)ncols) acc = fma(vals[k], x[c], acc);
-            else bad = true;
+        if (r < nrows) {
+            const long long s = row_ptr[r], e = row_ptr[r + 1];
+            for (long long k = s + sub; k < e; k += G) {
+                const long long c = (long long)col_idx[k];
+                if ((unsigned long long)c < (unsigned long long)ncols) acc = fma(vals[k], x[c], acc);
+                else bad = true;
+            }
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
-        if (sub == 0) y[r] = acc;
+        if (sub == 0 && r < nrows) y[r] = acc;
     }
     if (bad) raise_error(err, ERRBIT_BOUNDS);
 }
@@ -137,15 +146,6 @@ static int lanes_for(double avg) {
 }
 
 // ---------------------------------------------------------------- batched pipeline
-// Instance descriptor (device table).
-struct BatchInst {
-    long long nrows, ncols, nnz;
-    long long entry_base;  // first entry in the concatenated COO / CSR arrays
-    long long row_base;    // first row in the concatenated y / row counts
-    long long x_base;      // first element of this instance's x
-    long long rp_base;     // first element of this instance's row_ptr (= row_base + instance index)
-};
-
 struct WorkItem {
     int inst;
     int tile;  // tile index inside the instance
@@ -167,9 +167,8 @@ __device__ __forceinline__ bool next_item(unsigned* cursor, unsigned nitems, uns
 // Stage 1: row counts (and validation of every entry).
 __global__ void __launch_bounds__(kBatchThreads) batch_count_kernel(const BatchInst* __restrict__ inst,
                                                                     const WorkItem* __restrict__ items, unsigned nitems,
-                                                                    unsigned* cursor, const int* __restrict__ rows,
-                                                                    const int* __restrict__ cols,
-                                                                    unsigned* __restrict__ counts, unsigned* err) {
+                                                                    unsigned* cursor, unsigned* __restrict__ counts,
+                                                                    unsigned* err) {
     unsigned it;
     bool bad = false;
     while (next_item(cursor, nitems, it)) {
@@ -178,7 +177,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_count_kernel(const BatchI
         const long long t0 = (long long)w.tile * kEntryTile;
         const long long t1 = t0 + kEntryTile < I.nnz ? t0 + kEntryTile : I.nnz;
         for (long long k = t0 + threadIdx.x; k < t1; k += kBatchThreads) {
-            const int r = rows[I.entry_base + k], c = cols[I.entry_base + k];
+            const int r = I.rows[k], c = I.cols[k];
             if (r >= 0 && r < I.nrows && c >= 0 && c < I.ncols) atomicAdd(&counts[I.row_base + r], 1u);
             else bad = true;
         }
@@ -197,13 +196,8 @@ __global__ void widen_kernel(const unsigned* __restrict__ c, long long* __restri
 __global__ void __launch_bounds__(kBatchThreads) batch_scatter_kernel(const BatchInst* __restrict__ inst,
                                                                       const WorkItem* __restrict__ items,
                                                                       unsigned nitems, unsigned* cursor,
-                                                                      const int* __restrict__ rows,
-                                                                      const int* __restrict__ cols,
-                                                                      const double* __restrict__ vals,
                                                                       const long long* __restrict__ row_start,
-                                                                      unsigned* __restrict__ counts,
-                                                                      int* __restrict__ csr_cols,
-                                                                      double* __restrict__ csr_vals) {
+                                                                      unsigned* __restrict__ counts) {
     unsigned it;
     while (next_item(cursor, nitems, it)) {
         const WorkItem w = items[it];
@@ -211,14 +205,13 @@ __global__ void __launch_bounds__(kBatchThreads) batch_scatter_kernel(const Batc
         const long long t0 = (long long)w.tile * kEntryTile;
         const long long t1 = t0 + kEntryTile < I.nnz ? t0 + kEntryTile : I.nnz;
         for (long long k = t0 + threadIdx.x; k < t1; k += kBatchThreads) {
-            const long long e = I.entry_base + k;
-            const int r = rows[e], c = cols[e];
+            const int r = I.rows[k], c = I.cols[k];
             if (r < 0 || r >= I.nrows || c < 0 || c >= I.ncols) continue;  // reported by stage 1
             const long long g = I.row_base + r;
             const unsigned left = atomicSub(&counts[g], 1u);  // slots of row g still free
-            const long long slot = row_start[g] + (long long)left - 1;
-            csr_cols[slot] = c;
-            csr_vals[slot] = vals[e];
+            const long long slot = row_start[g] - I.scan_base + (long long)left - 1;
+            I.csr_cols[slot] = c;
+            I.csr_vals[slot] = I.vals[k];
         }
     }
 }
@@ -301,8 +294,7 @@ __device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* 
 // Also writes the instance's row_ptr (relative to its entry base).
 __global__ void __launch_bounds__(kBatchThreads) batch_sort_spmv_kernel(
     const BatchInst* __restrict__ inst, const WorkItem* __restrict__ items, unsigned nitems, unsigned* cursor,
-    const long long* __restrict__ row_start, int* __restrict__ csr_cols, double* __restrict__ csr_vals,
-    const double* __restrict__ x, long long* __restrict__ row_ptr, double* __restrict__ y, unsigned* err) {
+    const long long* __restrict__ row_start, unsigned* err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int W = kBatchThreads / 32;
     unsigned it;
@@ -314,24 +306,112 @@ __global__ void __launch_bounds__(kBatchThreads) batch_sort_spmv_kernel(
         const long long r1 = r0 + kRowTile < I.nrows ? r0 + kRowTile : I.nrows;
         for (long long r = r0 + warp; r < r1; r += W) {
             const long long g = I.row_base + r;
-            const long long s = row_start[g];
-            const long long e = (r + 1 < I.nrows) ? row_start[g + 1] : I.entry_base + I.nnz;
+            const long long s = row_start[g] - I.scan_base;
+            const long long e = (r + 1 < I.nrows) ? row_start[g + 1] - I.scan_base : I.nnz;
             const int len = (int)(e - s);
             if (lane == 0) {
-                row_ptr[I.rp_base + r] = s - I.entry_base;
-                if (r == I.nrows - 1) row_ptr[I.rp_base + I.nrows] = I.nnz;
+                I.row_ptr[r] = s;
+                if (r == I.nrows - 1) I.row_ptr[I.nrows] = I.nnz;
             }
-            int* cc = csr_cols + s;
-            double* cv = csr_vals + s;
-            const double* xi = x + I.x_base;
-            if (len <= 32) sort_row_and_spmv<1>(cc, cv, len, xi, y + g);
-            else if (len <= 64) sort_row_and_spmv<2>(cc, cv, len, xi, y + g);
-            else if (len <= 128) sort_row_and_spmv<4>(cc, cv, len, xi, y + g);
-            else if (len <= 256) sort_row_and_spmv<8>(cc, cv, len, xi, y + g);
+            int* cc = I.csr_cols + s;
+            double* cv = I.csr_vals + s;
+            if (len <= 32) sort_row_and_spmv<1>(cc, cv, len, I.x, I.y + r);
+            else if (len <= 64) sort_row_and_spmv<2>(cc, cv, len, I.x, I.y + r);
+            else if (len <= 128) sort_row_and_spmv<4>(cc, cv, len, I.x, I.y + r);
+            else if (len <= 256) sort_row_and_spmv<8>(cc, cv, len, I.x, I.y + r);
             else bad = true;  // rows above 256 entries are outside this kernel's contract
         }
     }
     if (bad) raise_error(err, ERRBIT_BOUNDS);
+}
+
+// Runs the four stages for a batch described by host-side `inst` (row_base and
+// scan_base filled here).  Scratch comes from the named device buffer `key`.
+// With `staging` (pinned host memory of `staging_bytes`, kept alive by the
+// caller until the stream reaches this point) the tables are copied
+// asynchronously and the call returns without synchronizing; otherwise it
+// synchronizes the stream before returning.
+int batch_pipeline(std::vector<BatchInst>& inst, const char* key, cudaStream_t s, void* staging,
+                   size_t staging_bytes) {
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    std::vector<WorkItem> count_items, row_items;
+    long long rows_total = 0, entries = 0;
+    for (size_t i = 0; i < inst.size(); ++i) {
+        BatchInst& I = inst[i];
+        I.row_base = rows_total;
+        I.scan_base = entries;
+        for (long long t = 0; t * kEntryTile < I.nnz; ++t) count_items.push_back(WorkItem{(int)i, (int)t});
+        for (long long t = 0; t * kRowTile < I.nrows; ++t) row_items.push_back(WorkItem{(int)i, (int)t});
+        rows_total += I.nrows;
+        entries += I.nnz;
+    }
+    if (rows_total >= (1LL << 32)) return set_error(HYD_CUDA_ERR_UNSUPPORTED, "batch: too many rows");
+    const size_t inst_bytes = (inst.size() * sizeof(BatchInst) + 255) & ~(size_t)255;
+    const size_t ci_bytes = ((count_items.size() * sizeof(WorkItem)) + 255) & ~(size_t)255;
+    const size_t ri_bytes = ((row_items.size() * sizeof(WorkItem)) + 255) & ~(size_t)255;
+    const size_t cnt_bytes = ((size_t)rows_total * 4 + 255) & ~(size_t)255;
+    const size_t wide_bytes = ((size_t)rows_total * 8 + 255) & ~(size_t)255;
+    void* buf = nullptr;
+    HYD_TRY(device_buffer(d, key, inst_bytes + ci_bytes + ri_bytes + cnt_bytes + 2 * wide_bytes + 256, &buf));
+    unsigned char* b = static_cast<unsigned char*>(buf);
+    BatchInst* d_inst = reinterpret_cast<BatchInst*>(b);
+    WorkItem* d_ci = reinterpret_cast<WorkItem*>(b + inst_bytes);
+    WorkItem* d_ri = reinterpret_cast<WorkItem*>(b + inst_bytes + ci_bytes);
+    unsigned* counts = reinterpret_cast<unsigned*>(b + inst_bytes + ci_bytes + ri_bytes);
+    long long* wide = reinterpret_cast<long long*>(b + inst_bytes + ci_bytes + ri_bytes + cnt_bytes);
+    long long* row_start = wide + (wide_bytes / 8);
+    unsigned* cursors = reinterpret_cast<unsigned*>(b + inst_bytes + ci_bytes + ri_bytes + cnt_bytes + 2 * wide_bytes);
+    const size_t table_bytes = inst_bytes + ci_bytes + ri_bytes;
+    const unsigned char* src_inst = reinterpret_cast<const unsigned char*>(inst.data());
+    const unsigned char* src_ci = reinterpret_cast<const unsigned char*>(count_items.data());
+    const unsigned char* src_ri = reinterpret_cast<const unsigned char*>(row_items.data());
+    const bool async_tables = staging != nullptr && staging_bytes >= table_bytes;
+    if (async_tables) {
+        unsigned char* h = static_cast<unsigned char*>(staging);
+        memcpy(h, src_inst, inst.size() * sizeof(BatchInst));
+        if (!count_items.empty()) memcpy(h + inst_bytes, src_ci, count_items.size() * sizeof(WorkItem));
+        memcpy(h + inst_bytes + ci_bytes, src_ri, row_items.size() * sizeof(WorkItem));
+        HYD_CUDA_TRY(cudaMemcpyAsync(b, h, table_bytes, cudaMemcpyHostToDevice, s));
+    } else {
+        HYD_CUDA_TRY(cudaMemcpyAsync(d_inst, src_inst, inst.size() * sizeof(BatchInst), cudaMemcpyHostToDevice, s));
+        if (!count_items.empty())
+            HYD_CUDA_TRY(cudaMemcpyAsync(d_ci, src_ci, count_items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
+        HYD_CUDA_TRY(cudaMemcpyAsync(d_ri, src_ri, row_items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
+    }
+    HYD_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)rows_total * 4, s));
+    HYD_CUDA_TRY(cudaMemsetAsync(cursors, 0, 16, s));
+    const unsigned grid = (unsigned)(d->sm_count * 8);
+    if (!count_items.empty()) {
+        batch_count_kernel<<<grid, kBatchThreads, 0, s>>>(d_inst, d_ci, (unsigned)count_items.size(), cursors + 0,
+                                                          counts, d->d_err);
+        HYD_TRY(launch_check("batch_count"));
+    }
+    widen_kernel<<<grid, 256, 0, s>>>(counts, wide, rows_total);
+    HYD_TRY(launch_check("batch_widen"));
+    HYD_TRY(scan_i64_launch(wide, row_start, rows_total, 0, false, false, s));
+    if (!count_items.empty()) {
+        batch_scatter_kernel<<<grid, kBatchThreads, 0, s>>>(d_inst, d_ci, (unsigned)count_items.size(), cursors + 1,
+                                                            row_start, counts);
+        HYD_TRY(launch_check("batch_scatter"));
+    }
+    batch_sort_spmv_kernel<<<grid, kBatchThreads, 0, s>>>(d_inst, d_ri, (unsigned)row_items.size(), cursors + 2,
+                                                          row_start, d->d_err);
+    HYD_TRY(launch_check("batch_sort_spmv"));
+    // pageable tables die with the caller's vectors: the copies must have run
+    if (!async_tables) HYD_CUDA_TRY(cudaStreamSynchronize(s));
+    return HYD_CUDA_OK;
+}
+
+// Bytes of pinned staging batch_pipeline needs for `inst` (0 if none).
+size_t batch_pipeline_table_bytes(const std::vector<BatchInst>& inst) {
+    size_t ci = 0, ri = 0;
+    for (const BatchInst& I : inst) {
+        ci += (size_t)((I.nnz + kEntryTile - 1) / kEntryTile);
+        ri += (size_t)((I.nrows + kRowTile - 1) / kRowTile);
+    }
+    return ((inst.size() * sizeof(BatchInst) + 255) & ~(size_t)255) + ((ci * sizeof(WorkItem) + 255) & ~(size_t)255) +
+           ((ri * sizeof(WorkItem) + 255) & ~(size_t)255);
 }
 
 }  // namespace hyd
@@ -451,69 +531,28 @@ extern "C" int hyd_cuda_batched_coo_csr_spmv_f64(int64_t ninst, const int64_t* d
     HYD_CHECK_ARG(ninst == 0 || desc != nullptr, "batched_coo_csr_spmv: null descriptor table");
     if (ninst == 0) return HYD_CUDA_OK;
     std::vector<BatchInst> inst((size_t)ninst);
-    std::vector<WorkItem> count_items, row_items;
     long long entries = 0, rows_total = 0, xs = 0;
     for (int64_t i = 0; i < ninst; ++i) {
         const long long nr = desc[3 * i], nc = desc[3 * i + 1], nz = desc[3 * i + 2];
         HYD_CHECK_ARG(nr >= 1 && nc >= 1 && nz >= 0 && nr < (1LL << 31) && nc < (1LL << 31),
                       "batched_coo_csr_spmv: instance %lld has a bad shape", (long long)i);
-        inst[i] = BatchInst{nr, nc, nz, entries, rows_total, xs, rows_total + i};
-        for (long long t = 0; t * kEntryTile < nz; ++t) count_items.push_back(WorkItem{(int)i, (int)t});
-        for (long long t = 0; t * kRowTile < nr; ++t) row_items.push_back(WorkItem{(int)i, (int)t});
+        BatchInst& I = inst[i];
+        I.nrows = nr;
+        I.ncols = nc;
+        I.nnz = nz;
+        I.rows = rows + entries;
+        I.cols = cols + entries;
+        I.vals = vals + entries;
+        I.x = x + xs;
+        I.row_ptr = (long long*)row_ptr + rows_total + i;
+        I.csr_cols = csr_cols + entries;
+        I.csr_vals = csr_vals + entries;
+        I.y = y + rows_total;
         entries += nz;
         rows_total += nr;
         xs += nc;
     }
     HYD_CHECK_ARG(entries == 0 || (rows && cols && vals && csr_cols && csr_vals), "batched_coo_csr_spmv: null entries");
     HYD_CHECK_ARG(x && y && row_ptr, "batched_coo_csr_spmv: null x / y / row_ptr");
-    HYD_CHECK_ARG(rows_total < (1LL << 32), "batched_coo_csr_spmv: too many rows");
-    cudaStream_t s = as_stream(stream);
-    Device* d = nullptr;
-    HYD_TRY(device(&d));
-    // device tables and scratch
-    const size_t inst_bytes = ((size_t)ninst * sizeof(BatchInst) + 255) & ~(size_t)255;
-    const size_t ci_bytes = ((count_items.size() * sizeof(WorkItem)) + 255) & ~(size_t)255;
-    const size_t ri_bytes = ((row_items.size() * sizeof(WorkItem)) + 255) & ~(size_t)255;
-    const size_t cnt_bytes = ((size_t)rows_total * 4 + 255) & ~(size_t)255;
-    const size_t wide_bytes = ((size_t)rows_total * 8 + 255) & ~(size_t)255;
-    void* buf = nullptr;
-    HYD_TRY(device_buffer(d, "batch_tables", inst_bytes + ci_bytes + ri_bytes + cnt_bytes + 2 * wide_bytes + 256, &buf));
-    unsigned char* b = static_cast<unsigned char*>(buf);
-    BatchInst* d_inst = reinterpret_cast<BatchInst*>(b);
-    WorkItem* d_ci = reinterpret_cast<WorkItem*>(b + inst_bytes);
-    WorkItem* d_ri = reinterpret_cast<WorkItem*>(b + inst_bytes + ci_bytes);
-    unsigned* counts = reinterpret_cast<unsigned*>(b + inst_bytes + ci_bytes + ri_bytes);
-    long long* wide = reinterpret_cast<long long*>(b + inst_bytes + ci_bytes + ri_bytes + cnt_bytes);
-    long long* row_start = wide + (wide_bytes / 8);
-    unsigned* cursors = reinterpret_cast<unsigned*>(b + inst_bytes + ci_bytes + ri_bytes + cnt_bytes + 2 * wide_bytes);
-    // the host tables must stay alive until the copies ran
-    HYD_CUDA_TRY(cudaMemcpyAsync(d_inst, inst.data(), inst.size() * sizeof(BatchInst), cudaMemcpyHostToDevice, s));
-    if (!count_items.empty())
-        HYD_CUDA_TRY(cudaMemcpyAsync(d_ci, count_items.data(), count_items.size() * sizeof(WorkItem),
-                                     cudaMemcpyHostToDevice, s));
-    HYD_CUDA_TRY(cudaMemcpyAsync(d_ri, row_items.data(), row_items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
-    HYD_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)rows_total * 4, s));
-    HYD_CUDA_TRY(cudaMemsetAsync(cursors, 0, 16, s));
-    const unsigned grid = (unsigned)(d->sm_count * 8);
-    if (!count_items.empty()) {
-        batch_count_kernel<<<grid, kBatchThreads, 0, s>>>(d_inst, d_ci, (unsigned)count_items.size(), cursors + 0,
-                                                          rows, cols, counts, d->d_err);
-        HYD_TRY(launch_check("batch_count"));
-    }
-    widen_kernel<<<grid, 256, 0, s>>>(counts, wide, rows_total);
-    HYD_TRY(launch_check("batch_widen"));
-    // global exclusive scan: row_start[g] = first entry slot of global row g
-    HYD_TRY(scan_i64_launch(wide, row_start, rows_total, 0, false, false, s));
-    if (!count_items.empty()) {
-        batch_scatter_kernel<<<grid, kBatchThreads, 0, s>>>(d_inst, d_ci, (unsigned)count_items.size(), cursors + 1,
-                                                            rows, cols, vals, row_start, counts, csr_cols, csr_vals);
-        HYD_TRY(launch_check("batch_scatter"));
-    }
-    batch_sort_spmv_kernel<<<grid, kBatchThreads, 0, s>>>(d_inst, d_ri, (unsigned)row_items.size(), cursors + 2,
-                                                          row_start, csr_cols, csr_vals, x, (long long*)row_ptr, y,
-                                                          d->d_err);
-    HYD_TRY(launch_check("batch_sort_spmv"));
-    // the host vectors die at return: make sure the H2D copies have consumed them
-    HYD_CUDA_TRY(cudaStreamSynchronize(s));
-    return HYD_CUDA_OK;
+    return batch_pipeline(inst, "batch_tables", as_stream(stream), nullptr, 0);
 }

@@ -63,6 +63,16 @@ SIGNATURES = {
     "hyd_cuda_spmv_csr_i32_f64": (_i, [_i64, _i64, _p, _p, _p, _p, _p, _i, _p]),
     "hyd_cuda_batched_coo_csr_spmv_f64": (_i, [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     "hyd_cuda_synth_coo_batch": (_i, [_i64, _u64, _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p]),
+    "hyd_cuda_server_create": (_i, [_p, C.POINTER(C.c_void_p)]),
+    "hyd_cuda_server_submit": (_i, [_p, _p, C.POINTER(C.c_int64)]),
+    "hyd_cuda_server_wait": (_i, [_p, _i64, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "hyd_cuda_server_stats": (_i, [_p, _p]),
+    "hyd_cuda_server_shutdown": (_i, [_p]),
+    "hyd_cuda_server_error": (C.c_char_p, [_p]),
+    "hyd_cuda_server_destroy": (_i, [_p]),
+    "hyd_cuda_request_run": (_i, [_p, _p]),
+    "hyd_cuda_serve_trace": (_i, [_p, _p, _p, _i64, _p, _p, C.POINTER(C.c_double)]),
+    "hyd_cuda_plain_trace": (_i, [_p, _p, _i64, _p, _p, C.POINTER(C.c_double), _p]),
     "hyd_cuda_weighted_histogram_host": (_i, [_p, _i64, _i64, _p, _i]),
     "hyd_cuda_dot_f64_host": (_i, [_p, _p, _i64, _p]),
     "hyd_cuda_array_alloc": (_p, [None, C.c_size_t]),
@@ -84,6 +94,27 @@ class Array(C.Structure):
     """hyd_array_t (runtime/hydrangea_runtime.h:230-235)."""
     _fields_ = [("storage", C.POINTER(Storage)), ("data", C.c_void_p), ("elem_size", C.c_size_t),
                 ("shape", Tuple)]
+
+
+REQ_DOT, REQ_HIST, REQ_LAPLACIAN, REQ_SPMV = 1, 2, 3, 4
+
+
+class Request(C.Structure):
+    """hyd_request_t."""
+    _fields_ = [("kind", C.c_int), ("n", C.c_int64), ("m", C.c_int64),
+                ("in0", C.c_void_p), ("in1", C.c_void_p), ("in2", C.c_void_p), ("in3", C.c_void_p),
+                ("out0", C.c_void_p), ("out1", C.c_void_p), ("out2", C.c_void_p), ("out3", C.c_void_p)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("streams", C.c_int), ("max_batch", C.c_int),
+                ("max_batch_bytes", C.c_int64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("rejected", C.c_int64), ("cancelled", C.c_int64), ("launches", C.c_int64),
+                ("peak_inflight_bytes", C.c_int64), ("inflight_bytes", C.c_int64), ("queued", C.c_int64)]
 
 
 class HydCudaError(RuntimeError):
@@ -289,6 +320,74 @@ def batched_coo_csr_spmv(desc, rows, cols, vals, x, stream=None):
     call("hyd_cuda_batched_coo_csr_spmv_f64", ninst, desc.ctypes.data, ptr(rows), ptr(cols), ptr(vals), ptr(x),
          ptr(row_ptr), ptr(csr_cols), ptr(csr_vals), ptr(y), stream_handle(stream))
     return row_ptr, csr_cols, csr_vals, y
+
+
+class Server:
+    """Thin owner of a hyd_server_t."""
+
+    def __init__(self, budget_bytes=0, streams=0, max_batch=0, max_batch_bytes=0):
+        cfg = ServerConfig(budget_bytes, streams, max_batch, max_batch_bytes)
+        h = C.c_void_p()
+        call("hyd_cuda_server_create", C.addressof(cfg), C.byref(h))
+        self.h = h
+
+    def submit(self, req):
+        t = C.c_int64(-1)
+        st = lib().hyd_cuda_server_submit(self.h, C.addressof(req), C.byref(t))
+        return st, t.value
+
+    def wait(self, ticket):
+        st = C.c_int(-1)
+        lat = C.c_double(0.0)
+        call("hyd_cuda_server_wait", self.h, ticket, C.byref(st), C.byref(lat))
+        return st.value, lat.value
+
+    def stats(self):
+        out = ServerStats()
+        call("hyd_cuda_server_stats", self.h, C.addressof(out))
+        return out
+
+    def trace(self, reqs, arrivals):
+        import numpy as np
+        n = len(reqs)
+        arr = (Request * n)(*reqs)
+        t = np.ascontiguousarray(arrivals, dtype=np.float64)
+        lat = np.zeros(n)
+        st = np.zeros(n, dtype=np.int32)
+        el = C.c_double(0.0)
+        call("hyd_cuda_serve_trace", self.h, C.addressof(arr), t.ctypes.data, n, lat.ctypes.data, st.ctypes.data,
+             C.byref(el))
+        return lat, st, el.value
+
+    def error(self):
+        return (lib().hyd_cuda_server_error(self.h) or b"").decode()
+
+    def shutdown(self):
+        call("hyd_cuda_server_shutdown", self.h)
+
+    def close(self):
+        if self.h:
+            lib().hyd_cuda_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def plain_trace(reqs, arrivals, stream=None):
+    import numpy as np
+    n = len(reqs)
+    arr = (Request * n)(*reqs)
+    t = np.ascontiguousarray(arrivals, dtype=np.float64)
+    lat = np.zeros(n)
+    st = np.zeros(n, dtype=np.int32)
+    el = C.c_double(0.0)
+    call("hyd_cuda_plain_trace", C.addressof(arr), t.ctypes.data, n, lat.ctypes.data, st.ctypes.data, C.byref(el),
+         stream_handle(stream))
+    return lat, st, el.value
 
 
 def make_array(np_array):

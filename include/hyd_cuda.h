@@ -249,6 +249,82 @@ int hyd_cuda_synth_coo_batch(int64_t ninst, uint64_t seed0, int min_log2, int ma
                              int64_t* desc, int32_t* rows, int32_t* cols, double* vals, double* x,
                              int64_t capacity_entries, void* stream);
 
+/* ---- serving --------------------------------------------------------------------
+ * A resident request server inside the runtime (no reference counterpart; the
+ * nearest are the memoised procedures of CodegenC.hs:690-707 and the Metal
+ * export lifecycle with cached device buffers, CodegenMSL.hs:1120-1181).
+ * Requests reference device-resident arrays.  Kinds and fields:
+ *   HYD_REQ_DOT        n elements; in0 xs, in1 ys (f64); out0 one f64
+ *   HYD_REQ_HIST       n elements, m bins (<= 8192); in0 data (i64); out0 hist
+ *                      (m int64, overwritten): the fused weighted histogram
+ *   HYD_REQ_LAPLACIAN  n rows, m cols; in0 grid, out0 grid (f64): one clamp
+ *                      Laplacian step (HYD_STENCIL_LAPLACIAN)
+ *   HYD_REQ_SPMV       n rows = cols, m entries; in0 rows, in1 cols (int32),
+ *                      in2 vals, in3 x (f64); out0 y, out1 row_ptr (n+1 int64),
+ *                      out2 csr cols (int32), out3 csr vals: COO -> CSR -> SpMV
+ *                      as hyd_cuda_batched_coo_csr_spmv_f64 for one instance.
+ * Admission: a request is admitted once the working sets in flight plus its own
+ * fit hbm_budget_bytes (FIFO); a request larger than the budget completes with
+ * HYD_CUDA_ERR_BUDGET.  Continuous batching: when a stream slot is free every
+ * admitted waiting request (up to max_batch / max_batch_bytes) joins one batch,
+ * dot/hist/Laplacian in a single persistent launch over (request, tile) work
+ * items, SpMV requests in the batched pipeline; slots overlap on the device.
+ * A request's result does not depend on what it was batched with.  Requests
+ * that may be in flight together must not write the same output arrays (their
+ * kernels would race, as any two overlapping launches would). */
+typedef enum { HYD_REQ_DOT = 1, HYD_REQ_HIST = 2, HYD_REQ_LAPLACIAN = 3, HYD_REQ_SPMV = 4 } hyd_request_kind_t;
+typedef struct {
+    int kind;
+    int64_t n;
+    int64_t m;
+    const void* in0;
+    const void* in1;
+    const void* in2;
+    const void* in3;
+    void* out0;
+    void* out1;
+    void* out2;
+    void* out3;
+} hyd_request_t;
+typedef struct {
+    int64_t hbm_budget_bytes;  /* 0: a quarter of the free device memory */
+    int streams;               /* launch slots in flight (0: 4) */
+    int max_batch;             /* requests per batch (0: 256) */
+    int64_t max_batch_bytes;   /* working set per batch (0: budget / streams) */
+} hyd_server_config_t;
+typedef struct {
+    int64_t submitted, completed, failed, rejected, cancelled;
+    int64_t launches;             /* batches issued */
+    int64_t peak_inflight_bytes;  /* never above hbm_budget_bytes */
+    int64_t inflight_bytes, queued;
+} hyd_server_stats_t;
+typedef struct hyd_server hyd_server_t;
+int hyd_cuda_server_create(const hyd_server_config_t* cfg, hyd_server_t** out);
+/* Non-blocking; returns the request's immediate status (a validation, budget
+ * or shutdown rejection) or HYD_CUDA_OK when queued.  *ticket is always set. */
+int hyd_cuda_server_submit(hyd_server_t* srv, const hyd_request_t* req, int64_t* ticket);
+/* Blocks until the ticket's request finished; status and latency
+ * (arrival -> result ready, seconds). */
+int hyd_cuda_server_wait(hyd_server_t* srv, int64_t ticket, int* status, double* latency_s);
+int hyd_cuda_server_stats(hyd_server_t* srv, hyd_server_stats_t* out);
+/* Message of the last batch that failed inside the server ("" if none). */
+const char* hyd_cuda_server_error(hyd_server_t* srv);
+/* Stops accepting work: queued requests complete with HYD_CUDA_ERR_CANCELLED,
+ * batches in flight finish; tickets stay queryable until destroy. */
+int hyd_cuda_server_shutdown(hyd_server_t* srv);
+/* Shutdown (if not done) and release every resource of the server. */
+int hyd_cuda_server_destroy(hyd_server_t* srv);
+/* The plain per-call path: one request, blocking, on `stream`. */
+int hyd_cuda_request_run(const hyd_request_t* req, void* stream);
+/* Trace drivers with native timing: submit reqs[i] at t0 + arrival_s[i]
+ * (seconds, ascending) and wait for all; latency_s[i] = arrival -> ready;
+ * *elapsed_s = t0 -> last completion.  serve_trace uses the server; plain_trace
+ * runs each request with hyd_cuda_request_run in arrival order. */
+int hyd_cuda_serve_trace(hyd_server_t* srv, const hyd_request_t* reqs, const double* arrival_s, int64_t n,
+                         double* latency_s, int* status, double* elapsed_s);
+int hyd_cuda_plain_trace(const hyd_request_t* reqs, const double* arrival_s, int64_t n, double* latency_s,
+                         int* status, double* elapsed_s, void* stream);
+
 /* ---- host-memory entry points (embedding boundary) --------------------------
  * Same computations on HOST pointers: the input is streamed to the device in
  * 64 MiB chunks on two streams (copy of chunk k+1 overlaps the kernel on chunk

@@ -40,3 +40,15 @@ def test_version_and_status_strings(hc):
 def test_invalid_arguments_rejected(hc, call):
     assert call(hc.lib()) == hc.ERR_INVALID
     assert hc.last_error()
+
+
+def test_server_requires_device_or_rejects_cleanly(hc):
+    import ctypes as C
+    import torch
+    L = hc.lib()
+    assert L.hyd_cuda_server_submit(None, None, None) == hc.ERR_INVALID
+    assert L.hyd_cuda_server_wait(None, 0, None, None) == hc.ERR_INVALID
+    assert L.hyd_cuda_request_run(None, None) == hc.ERR_INVALID
+    if not torch.cuda.is_available():
+        h = C.c_void_p()
+        assert L.hyd_cuda_server_create(None, C.byref(h)) == hc.ERR_NO_DEVICE
