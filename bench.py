@@ -42,6 +42,9 @@ def parse_args():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="histogram", choices=["histogram"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-suite", action="store_true",
+                   help="skip the other configurations (dot, heat_2d, batched, serving)")
+    p.add_argument("--serve-requests", type=int, default=100_000)
     return p.parse_args()
 
 
@@ -252,6 +255,12 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(host)
+    del pinned, out_host
+    suite = None
+    if rank == 0 and world == 1 and not args.no_suite:
+        del data, hists
+        torch.cuda.empty_cache()
+        suite = run_suite(hc, torch, args, measured_peak()[0])
 
     if rank == 0:
         line = {
@@ -301,9 +310,289 @@ def run_gpu(args):
         }
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if suite is not None:
+            line["suite"] = suite
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------------
+# The other configurations, measured after the headline (one JSON object each).
+# Correctness guards here use product code and size-independent properties; the
+# oracle only appears in the *_cpu_baseline helpers.
+# ----------------------------------------------------------------------------------
+FP64_DFMA_PER_S = 1.9 * 152 * 2.07e9  # measured on this GB300: 1.9 DFMA/clk/SM (1.2 TFLOP/s)
+
+
+def _events(torch, stream):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def suite_dot(hc, torch, peak, steps=50):
+    n = 1 << 24
+    dev = torch.device("cuda")
+    xs = torch.empty(n, dtype=torch.float64, device=dev)
+    ys = torch.empty(n, dtype=torch.float64, device=dev)
+    hc.fill_uniform_f64(xs, 1, -1.0, 1.0)
+    hc.fill_uniform_f64(ys, 2, -1.0, 1.0)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        hc.dot_f64(xs, ys, out)
+    first = out.item()
+    e0, e1 = _events(torch, s)
+    e0.record(s)
+    for _ in range(steps):
+        hc.dot_f64(xs, ys, out)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    assert out.item() == first  # run-to-run bit-identical
+    gbs = (16 * n + 8) / (ms / 1e3) / 1e9
+    res = {"config": "dot reduce(+) 0.0 (zipwith (*) xs ys), N=2^24 f64, U[-1,1) seeds 1,2",
+           "ms": round(ms, 5), "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3),
+           "launches_per_step": 1, "result": first}
+    try:
+        from oracle import oracle as O
+        res["cpu_baseline"] = _dot_cpu_baseline(O, xs.cpu().numpy(), ys.cpu().numpy(), first)
+    except Exception as e:  # the baseline is optional
+        res["cpu_baseline"] = {"error": str(e)}
+    return res
+
+
+def _dot_cpu_baseline(O, hx, hy, gpu_value):
+    ref = O.dot_compensated(hx, hy)
+    t = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t < 2.0:
+        O.dot(hx, hy)
+        reps += 1
+    dt = (time.perf_counter() - t) / reps
+    return {"value": round(16 * len(hx) / dt / 1e9, 2), "unit": "GB/s", "cores": O.lib().orc_max_threads(),
+            "kind": "port", "sample": "full N, %d reps" % reps,
+            "gpu_rel_err_vs_compensated": abs(gpu_value - ref) / max(1.0, abs(ref))}
+
+
+def suite_heat(hc, torch, peak, iters=1000):
+    h = w = 8192
+    dev = torch.device("cuda")
+    b0 = torch.empty((h, w), dtype=torch.float64, device=dev)
+    b1 = torch.empty_like(b0)
+    init = torch.empty_like(b0)
+    hc.fill_uniform_f64(init, 3, 0.0, 1.0)
+    best, times = hc.autotune_stencil2d(hc.STENCIL_HEAT, h, w, reps=5)
+    side = torch.cuda.Stream()
+    results = {}
+    outs = {}
+    for name, variant in (("autotuned", best), ("fixed_32x32", 0)):
+        b0.copy_(init)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            hc.iterate_stencil2d(hc.STENCIL_HEAT, b0, b1, iters, stream=side, variant=variant)  # builds the graph
+        side.synchronize()
+        b0.copy_(init)
+        torch.cuda.synchronize()
+        e0, e1 = _events(torch, side)
+        with torch.cuda.stream(side):
+            e0.record(side)
+            res = hc.iterate_stencil2d(hc.STENCIL_HEAT, b0, b1, iters, stream=side, variant=variant)
+            e1.record(side)
+        side.synchronize()
+        ms = e0.elapsed_time(e1)
+        results[name] = {"variant": variant, "tile": str(hc.STENCIL_VARIANTS[variant]), "total_ms": round(ms, 2),
+                         "ms_per_step": round(ms / iters, 4)}
+        outs[name] = res.clone()
+    same = bool(torch.equal(outs["autotuned"], outs["fixed_32x32"]))
+    # one more step of the final state on two different variants must agree bit for bit
+    pts = h * w
+    ms_step = results["autotuned"]["ms_per_step"]
+    hbm = 16 * pts / (ms_step / 1e3) / 1e9
+    dp_ops = 6 * pts  # 3 DADD + fma(-4,e,t) + DMUL + DADD per point, bit-exact order
+    return {"config": "heat_2d out = in + 0.1*lap(in), clamp, 8192^2 f64 U[0,1) seed 3, 1000 steps, CUDA graph",
+            "steps": iters, "autotuned": results["autotuned"], "fixed_32x32": results["fixed_32x32"],
+            "tune_times_us_per_variant": {str(hc.STENCIL_VARIANTS[i]): round(float(t), 1) for i, t in enumerate(times)},
+            "speedup_vs_fixed_32x32": round(results["fixed_32x32"]["total_ms"] / results["autotuned"]["total_ms"], 3),
+            "variants_bit_identical_after_1000_steps": same,
+            "effective_hbm_GB_s": round(hbm, 1), "frac_of_hbm_peak": round(hbm / peak, 3),
+            "roofline": {"bound": "fp64", "achieved_dfma_equiv_per_s": round(dp_ops / (ms_step / 1e3), 3),
+                         "peak_dp_ops_per_s": FP64_DFMA_PER_S,
+                         "frac": round(dp_ops / (ms_step / 1e3) / FP64_DFMA_PER_S, 3),
+                         "note": "6 FP64 pipe ops per point; measured 1.9 DFMA/clk/SM on this GB300"}}
+
+
+def suite_batched(hc, torch, peak, steps=5):
+    import numpy as np
+    desc, rows, cols, vals, x = hc.synth_coo_batch(512, seed0=4, min_log2=10, max_log2=18, max_row_len=256)
+    nnz = int(desc[:, 2].sum())
+    n = int(desc[:, 0].sum())
+    torch.cuda.synchronize()
+    out = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)  # warm-up (allocates scratch)
+    hc.check(hc.device_check())
+    ts = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        out = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)  # synchronous
+        ts.append(time.perf_counter() - t)
+    ms = 1e3 * min(ts)
+    row_ptr = out[0].cpu().numpy()
+    # invariants: per instance row_ptr starts at 0, ends at nnz, is monotone
+    ok = True
+    p = 0
+    for nr, _, nz in desc:
+        rp = row_ptr[p:p + nr + 1]
+        ok &= rp[0] == 0 and rp[-1] == nz and bool(np.all(np.diff(rp) >= 0))
+        p += nr + 1
+    alg = 40 * nnz + 32 * n  # COO->CSR read 16 nnz + write 12 nnz + 4(n+1); SpMV 12 nnz + 4(n+1) + 8n + 8n
+    gbs = alg / (ms / 1e3) / 1e9
+    res = {"config": "512 instances seeds 4+i, n=2^U(10,18), Zipf(1.5) rows <= 256, int32 rows/cols, f64 vals/x",
+           "instances": 512, "nnz": nnz, "rows": n, "ms": round(ms, 3), "launches": "one persistent pass per stage",
+           "algorithmic_bytes": alg, "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3),
+           "csr_invariants_ok": bool(ok)}
+    try:
+        from oracle import oracle as O
+        res["cpu_baseline"] = _batched_cpu_baseline(O, desc, rows, cols, vals, x, alg / nnz)
+    except Exception as e:
+        res["cpu_baseline"] = {"error": str(e)}
+    return res
+
+
+def _batched_cpu_baseline(O, desc, rows, cols, vals, x, bytes_per_entry, budget_s=10.0):
+    h_r, h_c, h_v, h_x = (t.cpu().numpy() for t in (rows, cols, vals, x))
+    e0 = xr = 0
+    done_nnz = 0
+    t = time.perf_counter()
+    k = 0
+    for n, nc, nz in desc:
+        O.coo_to_csr_spmv(n, nc, h_r[e0:e0 + nz], h_c[e0:e0 + nz], h_v[e0:e0 + nz], h_x[xr:xr + nc])
+        e0 += nz
+        xr += nc
+        done_nnz += nz
+        k += 1
+        if time.perf_counter() - t > budget_s:
+            break
+    dt = time.perf_counter() - t
+    return {"value": round(done_nnz * bytes_per_entry / dt / 1e9, 3), "unit": "GB/s",
+            "cores": O.lib().orc_max_threads(), "kind": "port",
+            "sample": "first %d of 512 instances (%d entries), serial radix sort + scan + OpenMP SpMV" % (k, done_nnz)}
+
+
+def _serve_pool(hc, torch, per_kind=256, seed=5):
+    """Device-resident inputs/outputs: per kind `per_kind` entries with sizes drawn
+    from the workload's distributions; request i of a kind uses entry
+    (its index mod per_kind), so no two requests in flight share outputs."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    dev = torch.device("cuda")
+    keep = []
+    pool = {1: [], 2: [], 3: [], 4: []}
+    for j in range(per_kind):
+        n = int(2 ** rng.uniform(12, 24))
+        xs = torch.empty(n, dtype=torch.float64, device=dev)
+        ys = torch.empty(n, dtype=torch.float64, device=dev)
+        hc.fill_uniform_f64(xs, 1000 + j, -1.0, 1.0)
+        hc.fill_uniform_f64(ys, 2000 + j, -1.0, 1.0)
+        out = torch.zeros(1, dtype=torch.float64, device=dev)
+        keep += [xs, ys, out]
+        pool[1].append(hc.Request(hc.REQ_DOT, n, 0, xs.data_ptr(), ys.data_ptr(), None, None, out.data_ptr()))
+        n = int(2 ** rng.uniform(12, 24))
+        bins = 64 if rng.uniform() < 0.5 else 4096
+        data = torch.empty(n, dtype=torch.int64, device=dev)
+        hc.fill_uniform_i64(data, 3000 + j, 1 << 20)
+        hist = torch.zeros(bins, dtype=torch.int64, device=dev)
+        keep += [data, hist]
+        pool[2].append(hc.Request(hc.REQ_HIST, n, bins, data.data_ptr(), None, None, None, hist.data_ptr()))
+        side = int(2 ** rng.uniform(8, 12))
+        g = torch.empty((side, side), dtype=torch.float64, device=dev)
+        hc.fill_uniform_f64(g, 4000 + j, 0.0, 1.0)
+        o = torch.empty_like(g)
+        keep += [g, o]
+        pool[3].append(hc.Request(hc.REQ_LAPLACIAN, side, side, g.data_ptr(), None, None, None, o.data_ptr()))
+    desc, rows, cols, vals, x = hc.synth_coo_batch(per_kind, seed0=5000, min_log2=10, max_log2=18, max_row_len=256)
+    keep += [rows, cols, vals, x]
+    e0 = xr = 0
+    for nr, nc, nz in desc:
+        y = torch.zeros(nr, dtype=torch.float64, device=dev)
+        rp = torch.zeros(nr + 1, dtype=torch.int64, device=dev)
+        cc = torch.zeros(max(nz, 1), dtype=torch.int32, device=dev)
+        cv = torch.zeros(max(nz, 1), dtype=torch.float64, device=dev)
+        keep += [y, rp, cc, cv]
+        pool[4].append(hc.Request(hc.REQ_SPMV, int(nr), int(nz), rows.data_ptr() + 4 * e0, cols.data_ptr() + 4 * e0,
+                                  vals.data_ptr() + 8 * e0, x.data_ptr() + 8 * xr, y.data_ptr(), rp.data_ptr(),
+                                  cc.data_ptr(), cv.data_ptr()))
+        e0 += int(nz)
+        xr += int(nc)
+    torch.cuda.synchronize()
+    return pool, keep
+
+
+def _trace(pool, nreq, lam, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    kinds = rng.integers(1, 5, size=nreq)
+    counters = {1: 0, 2: 0, 3: 0, 4: 0}
+    reqs = []
+    for k in kinds:
+        k = int(k)
+        reqs.append(pool[k][counters[k] % len(pool[k])])
+        counters[k] += 1
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, size=nreq)) if lam else np.zeros(nreq)
+    return reqs, arrivals
+
+
+def _lat_stats(lat, st, elapsed):
+    import numpy as np
+    ok = st == 0
+    return {"req_per_s": round(int(ok.sum()) / elapsed, 1), "p50_ms": round(1e3 * float(np.percentile(lat[ok], 50)), 3),
+            "p99_ms": round(1e3 * float(np.percentile(lat[ok], 99)), 3), "failed": int((~ok).sum()),
+            "elapsed_s": round(elapsed, 3)}
+
+
+def suite_serve(hc, torch, peak, nreq=100_000, lam=20_000.0):
+    pool, keep = _serve_pool(hc, torch)
+    reqs, arr = _trace(pool, nreq, lam, 5)
+    budget = 16 << 30
+    srv = hc.Server(budget_bytes=budget, streams=4, max_batch=32)
+    try:
+        lat_s, st_s, el_s = srv.trace(reqs, arr)
+        stats = srv.stats()
+    finally:
+        srv.close()
+    served = _lat_stats(lat_s, st_s, el_s)
+    served.update({"launches": int(stats.launches), "peak_inflight_bytes": int(stats.peak_inflight_bytes),
+                   "hbm_budget_bytes": budget})
+    lat_p, st_p, el_p = hc.plain_trace(reqs, arr)
+    plain = _lat_stats(lat_p, st_p, el_p)
+    # saturation: everything arrives at once
+    nsat = min(nreq, 20_000)
+    sreqs, sarr = _trace(pool, nsat, 0, 6)
+    srv = hc.Server(budget_bytes=budget, streams=4, max_batch=32)
+    try:
+        l1, s1, e1 = srv.trace(sreqs, sarr)
+    finally:
+        srv.close()
+    l2, s2, e2 = hc.plain_trace(sreqs, sarr)
+    sat_served, sat_plain = _lat_stats(l1, s1, e1), _lat_stats(l2, s2, e2)
+    return {"config": "Poisson lambda=20k req/s, %d requests (seed 5), uniform over {dot, hist B in {64,4096}, "
+                      "laplacian side 2^U(8,12), spmv instance}; dot/hist N=2^U(12,24); arrays device-resident"
+                      % nreq,
+            "served": served, "plain_per_call": plain,
+            "saturation": {"requests": nsat, "served": sat_served, "plain_per_call": sat_plain,
+                           "throughput_ratio": round(sat_served["req_per_s"] / max(sat_plain["req_per_s"], 1e-9), 2)}}
+
+
+def run_suite(hc, torch, args, peak):
+    out = {}
+    for name, fn in (("dot", suite_dot), ("heat_2d", suite_heat), ("batched_coo_csr_spmv", suite_batched),
+                     ("serving", lambda a, b, c: suite_serve(a, b, c, nreq=args.serve_requests))):
+        t = time.perf_counter()
+        try:
+            out[name] = fn(hc, torch, peak)
+        except Exception as e:  # one failing leg must not lose the headline line
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+        out[name]["wall_s"] = round(time.perf_counter() - t, 1)
+        torch.cuda.empty_cache()
+    return out
 
 
 def cpu_baseline(host_data, budget_s=20.0):

@@ -504,6 +504,12 @@ static int plan_hist(const Device* d, long long bins, int strategy, bool packabl
     p->ept = 0;
     p->smem = 0;
     if (strategy == HYD_SCATTER_AUTO) {
+        const int tuned = tune_lookup_hist(bins);
+        if (tuned >= HYD_SCATTER_SMEM_WARP && tuned <= HYD_SCATTER_GLOBAL &&
+            (tuned != HYD_SCATTER_CLUSTER || packable))
+            strategy = tuned;
+    }
+    if (strategy == HYD_SCATTER_AUTO) {
         if (bytes * 4 <= half) {
             strategy = HYD_SCATTER_SMEM_WARP;
         } else if (bytes <= optin) {

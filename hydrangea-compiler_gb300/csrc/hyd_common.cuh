@@ -89,6 +89,10 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 // sizes) for kernel `fn` on device `d`, once per (kernel, device).
 int configure_kernel(const void* fn, const Device* d, bool nonportable_cluster);
 
+// Autotuner table lookups (-1 when the shape class was never tuned).
+int tune_lookup_stencil(int kind, int64_t h, int64_t w);
+int tune_lookup_hist(int64_t bins);
+
 // Kernel launch error check after a <<<>>> launch.
 inline int launch_check(const char* what) {
     cudaError_t e = cudaGetLastError();

@@ -72,15 +72,25 @@ __global__ void __launch_bounds__(256) stencil_plain_kernel(const double* __rest
 }
 
 // ---------------------------------------------------------------- TMA path
-constexpr int kTH = 16;                 // output rows per tile
-constexpr int kTW = 128;                // output columns per tile
-constexpr int kBoxW = kTW + 4;          // input box columns (2-column halo each side)
-constexpr int kBoxH = kTH + 2;          // input box rows
+// Tile shapes: TH output rows x TW output columns, 256 threads, TW in {32, 64,
+// 128} so that a thread owns one column of TH*TW/256 consecutive rows.  The
+// input box adds a 1-row halo above/below and a 2-column halo left/right (the
+// TMA x coordinate must stay 16-byte aligned).
 constexpr int kStThreads = 256;
-constexpr int kRowsPerThread = kTH * kTW / kStThreads;  // 8
-constexpr int kStageBytes = kBoxW * kBoxH * 8;          // 19008
-constexpr int kStageStride = (kStageBytes + 1023) & ~1023;
-constexpr unsigned kTmaWaitLimit = 1u << 22;            // polls before a wait gives up
+constexpr unsigned kTmaWaitLimit = 1u << 22;  // polls before a wait gives up
+
+template <int TH, int TW>
+struct TileShape {
+    static constexpr int kBoxW = TW + 4;
+    static constexpr int kBoxH = TH + 2;
+    static constexpr int kRowsPerThread = TH * TW / kStThreads;
+    static constexpr int kStageBytes = kBoxW * kBoxH * 8;
+    static constexpr int kStageStride = (kStageBytes + 1023) & ~1023;
+    static constexpr size_t kSmem = 2 * (size_t)kStageStride + 64 + 1024;
+    static_assert(TW == 32 || TW == 64 || TW == 128, "TW must divide the thread count");
+    static_assert(TH * TW % kStThreads == 0 && kRowsPerThread >= 1, "tile must cover the threads");
+    static_assert(kBoxW <= 256 && kBoxH <= 256, "TMA box limit");
+};
 
 __device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
@@ -117,10 +127,15 @@ __device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap* map
         : "memory");
 }
 
-template <int KIND>
+template <int KIND, int kTH, int kTW>
 __global__ void __launch_bounds__(kStThreads)
     stencil_tma_kernel(const __grid_constant__ CUtensorMap in_map, double* __restrict__ out,
                        int h, int w, unsigned* err) {
+    using S = TileShape<kTH, kTW>;
+    constexpr int kBoxW = S::kBoxW;
+    constexpr int kStageBytes = S::kStageBytes;
+    constexpr int kStageStride = S::kStageStride;
+    constexpr int kRowsPerThread = S::kRowsPerThread;
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     // stages at 1024-byte aligned offsets, barriers after them
     unsigned char* base = reinterpret_cast<unsigned char*>(
@@ -210,7 +225,6 @@ __global__ void __launch_bounds__(kStThreads)
     }
 }
 
-constexpr size_t kTmaSmem = 2 * kStageStride + 64 + 1024;
 
 // --- driver entry point for tensor-map encoding --------------------------------------
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -234,10 +248,10 @@ static bool tma_ok(const double* p, int64_t h, int64_t w) {
            w >= 2 && h >= 1 && w <= (1LL << 31) - 1 && h <= (1LL << 31) - 1;
 }
 
-static int make_map(CUtensorMap* map, const double* p, int64_t h, int64_t w) {
+static int make_map(CUtensorMap* map, const double* p, int64_t h, int64_t w, int box_w, int box_h) {
     cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)h};
     cuuint64_t strides[1] = {(cuuint64_t)w * 8};
-    cuuint32_t box[2] = {(cuuint32_t)kBoxW, (cuuint32_t)kBoxH};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(p), dims, strides, box,
                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -246,34 +260,72 @@ static int make_map(CUtensorMap* map, const double* p, int64_t h, int64_t w) {
     return HYD_CUDA_OK;
 }
 
+// Tile variants (index = the autotuner's choice): 0 is the reference's fixed
+// 32 x 32 polyhedral tile (Polyhedral.hs:196-204), the others GPU-shaped.
+struct TileVariant {
+    int th, tw;
+};
+static const TileVariant kTiles[] = {{32, 32}, {16, 128}, {16, 64}, {32, 64}, {8, 128}, {32, 128}};
+constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
+constexpr int kPlainVariant = kNumTiles;  // the non-TMA kernel
+constexpr int kDefaultTile = 1;           // 16 x 128
+
+template <int KIND, int TH, int TW>
+static int launch_tma(const CUtensorMap* map, double* out, int64_t h, int64_t w, const Device* d, cudaStream_t stream) {
+    using S = TileShape<TH, TW>;
+    auto k = stencil_tma_kernel<KIND, TH, TW>;
+    HYD_TRY(configure_kernel((const void*)k, d, false));
+    const int64_t ntiles = ((h + TH - 1) / TH) * ((w + TW - 1) / TW);
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kStThreads, S::kSmem);
+    if (occ < 1) occ = 1;
+    int64_t grid = (int64_t)d->sm_count * occ;
+    if (grid > ntiles) grid = ntiles;
+    k<<<(unsigned)grid, kStThreads, S::kSmem, stream>>>(*map, out, (int)h, (int)w, d->d_err);
+    return HYD_CUDA_OK;
+}
+
 template <int KIND>
 static int launch_step_kind(const CUtensorMap* map, const double* in, double* out, int64_t h, int64_t w,
-                            bool tma, const Device* d, cudaStream_t stream) {
-    if (tma) {
-        auto k = stencil_tma_kernel<KIND>;
-        HYD_TRY(configure_kernel((const void*)k, d, false));
-        const int64_t ntiles = ((h + kTH - 1) / kTH) * ((w + kTW - 1) / kTW);
-        int occ = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kStThreads, kTmaSmem);
-        if (occ < 1) occ = 1;
-        int64_t grid = (int64_t)d->sm_count * occ;
-        if (grid > ntiles) grid = ntiles;
-        k<<<(unsigned)grid, kStThreads, kTmaSmem, stream>>>(*map, out, (int)h, (int)w, d->d_err);
-    } else {
-        dim3 grid((unsigned)((w + 31) / 32), (unsigned)((h + 7) / 8));
-        stencil_plain_kernel<KIND><<<grid, 256, 0, stream>>>(in, out, h, w);
+                            int variant, const Device* d, cudaStream_t stream) {
+    switch (variant) {
+        case 0: HYD_TRY((launch_tma<KIND, 32, 32>(map, out, h, w, d, stream))); break;
+        case 1: HYD_TRY((launch_tma<KIND, 16, 128>(map, out, h, w, d, stream))); break;
+        case 2: HYD_TRY((launch_tma<KIND, 16, 64>(map, out, h, w, d, stream))); break;
+        case 3: HYD_TRY((launch_tma<KIND, 32, 64>(map, out, h, w, d, stream))); break;
+        case 4: HYD_TRY((launch_tma<KIND, 8, 128>(map, out, h, w, d, stream))); break;
+        case 5: HYD_TRY((launch_tma<KIND, 32, 128>(map, out, h, w, d, stream))); break;
+        default: {
+            dim3 grid((unsigned)((w + 31) / 32), (unsigned)((h + 7) / 8));
+            stencil_plain_kernel<KIND><<<grid, 256, 0, stream>>>(in, out, h, w);
+        }
     }
     return launch_check("stencil2d_f64");
 }
 
 static int launch_step(int kind, const CUtensorMap* map, const double* in, double* out, int64_t h, int64_t w,
-                       bool tma, const Device* d, cudaStream_t stream) {
+                       int variant, const Device* d, cudaStream_t stream) {
     switch (kind) {
-        case ST_LAPLACIAN: return launch_step_kind<ST_LAPLACIAN>(map, in, out, h, w, tma, d, stream);
-        case ST_JACOBI: return launch_step_kind<ST_JACOBI>(map, in, out, h, w, tma, d, stream);
-        case ST_HEAT: return launch_step_kind<ST_HEAT>(map, in, out, h, w, tma, d, stream);
-        default: return launch_step_kind<ST_HEAT_EXAMPLE>(map, in, out, h, w, tma, d, stream);
+        case ST_LAPLACIAN: return launch_step_kind<ST_LAPLACIAN>(map, in, out, h, w, variant, d, stream);
+        case ST_JACOBI: return launch_step_kind<ST_JACOBI>(map, in, out, h, w, variant, d, stream);
+        case ST_HEAT: return launch_step_kind<ST_HEAT>(map, in, out, h, w, variant, d, stream);
+        default: return launch_step_kind<ST_HEAT_EXAMPLE>(map, in, out, h, w, variant, d, stream);
     }
+}
+
+// Variant for (kind, h, w): the autotuner's cached choice, else the default;
+// shapes TMA cannot describe always take the plain kernel.
+static int choose_variant(int kind, const double* a, const double* b, int64_t h, int64_t w, int forced) {
+    const bool tma = tma_ok(a, h, w) && (b == nullptr || tma_ok(b, h, w));
+    if (!tma) return kPlainVariant;
+    if (forced >= 0 && forced <= kPlainVariant) return forced;
+    const int t = tune_lookup_stencil(kind, h, w);
+    return t >= 0 && t <= kPlainVariant ? t : kDefaultTile;
+}
+
+static int maps_for(int variant, const double* p, int64_t h, int64_t w, CUtensorMap* map) {
+    if (variant >= kNumTiles) return HYD_CUDA_OK;
+    return make_map(map, p, h, w, kTiles[variant].tw + 4, kTiles[variant].th + 2);
 }
 
 // Cached executable graphs of whole `iterate` runs.
@@ -293,47 +345,52 @@ static std::map<GraphKey, cudaGraphExec_t> g_graphs;
 
 using namespace hyd;
 
-extern "C" int hyd_cuda_stencil2d_f64(int kind, const double* in, double* out, int64_t h, int64_t w,
-                                      void* stream) {
+extern "C" int hyd_cuda_stencil2d_f64_variant(int kind, const double* in, double* out, int64_t h, int64_t w,
+                                              int variant, void* stream) {
     HYD_CHECK_ARG(kind >= 0 && kind <= 3, "stencil2d: unknown kind %d", kind);
     HYD_CHECK_ARG(h >= 0 && w >= 0, "stencil2d: negative shape");
     HYD_CHECK_ARG(h * w == 0 || (in != nullptr && out != nullptr), "stencil2d: null buffer");
     HYD_CHECK_ARG(in != out || h * w == 0, "stencil2d: input and output must differ");
+    HYD_CHECK_ARG(variant >= -1 && variant <= kPlainVariant, "stencil2d: unknown variant %d", variant);
     if (h == 0 || w == 0) return HYD_CUDA_OK;
     Device* d = nullptr;
     HYD_TRY(device(&d));
-    const bool tma = tma_ok(in, h, w);
+    const int v = choose_variant(kind, in, nullptr, h, w, variant);
     CUtensorMap map;
-    if (tma) HYD_TRY(make_map(&map, in, h, w));
-    return launch_step(kind, &map, in, out, h, w, tma, d, as_stream(stream));
+    HYD_TRY(maps_for(v, in, h, w, &map));
+    return launch_step(kind, &map, in, out, h, w, v, d, as_stream(stream));
 }
 
-extern "C" int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
-                                              int64_t iters, int* final_buf, void* stream) {
+extern "C" int hyd_cuda_stencil2d_f64(int kind, const double* in, double* out, int64_t h, int64_t w,
+                                      void* stream) {
+    return hyd_cuda_stencil2d_f64_variant(kind, in, out, h, w, -1, stream);
+}
+
+extern "C" int hyd_cuda_iterate_stencil2d_f64_variant(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
+                                                      int64_t iters, int variant, int* final_buf, void* stream) {
     HYD_CHECK_ARG(kind >= 0 && kind <= 3, "iterate_stencil2d: unknown kind %d", kind);
     HYD_CHECK_ARG(h >= 0 && w >= 0 && iters >= 0, "iterate_stencil2d: negative shape or count");
     HYD_CHECK_ARG(final_buf != nullptr, "iterate_stencil2d: null final_buf");
     HYD_CHECK_ARG(h * w == 0 || (buf0 != nullptr && buf1 != nullptr && buf0 != buf1),
                   "iterate_stencil2d: need two distinct buffers");
+    HYD_CHECK_ARG(variant >= -1 && variant <= kPlainVariant, "iterate_stencil2d: unknown variant %d", variant);
     *final_buf = (int)(iters & 1);
     if (h == 0 || w == 0 || iters == 0) return HYD_CUDA_OK;
     Device* d = nullptr;
     HYD_TRY(device(&d));
     cudaStream_t st = as_stream(stream);
-    const bool tma = tma_ok(buf0, h, w) && tma_ok(buf1, h, w);
+    const int v = choose_variant(kind, buf0, buf1, h, w, variant);
     CUtensorMap maps[2];
-    if (tma) {
-        HYD_TRY(make_map(&maps[0], buf0, h, w));
-        HYD_TRY(make_map(&maps[1], buf1, h, w));
-    }
+    HYD_TRY(maps_for(v, buf0, h, w, &maps[0]));
+    HYD_TRY(maps_for(v, buf1, h, w, &maps[1]));
     double* bufs[2] = {buf0, buf1};
     // Graph capture needs a non-default stream; on the legacy stream run eagerly.
     if (st == nullptr || iters < 4) {
         for (int64_t t = 0; t < iters; ++t)
-            HYD_TRY(launch_step(kind, &maps[t & 1], bufs[t & 1], bufs[(t + 1) & 1], h, w, tma, d, st));
+            HYD_TRY(launch_step(kind, &maps[t & 1], bufs[t & 1], bufs[(t + 1) & 1], h, w, v, d, st));
         return HYD_CUDA_OK;
     }
-    GraphKey key{kind, h, w, iters, buf0, buf1, st};
+    GraphKey key{kind * 16 + v, h, w, iters, buf0, buf1, st};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_graph_mu);
@@ -342,13 +399,13 @@ extern "C" int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* bu
     }
     if (!exec) {
         // warm the per-kernel configuration outside capture
-        HYD_TRY(launch_step(kind, &maps[0], bufs[0], bufs[1], h, w, tma, d, st));
+        HYD_TRY(launch_step(kind, &maps[0], bufs[0], bufs[1], h, w, v, d, st));
         HYD_CUDA_TRY(cudaStreamSynchronize(st));
         cudaGraph_t graph = nullptr;
         HYD_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         int status = HYD_CUDA_OK;
         for (int64_t t = 0; t < iters && status == HYD_CUDA_OK; ++t)
-            status = launch_step(kind, &maps[t & 1], bufs[t & 1], bufs[(t + 1) & 1], h, w, tma, d, st);
+            status = launch_step(kind, &maps[t & 1], bufs[t & 1], bufs[(t + 1) & 1], h, w, v, d, st);
         cudaError_t ce = cudaStreamEndCapture(st, &graph);
         if (status != HYD_CUDA_OK) {
             if (graph) cudaGraphDestroy(graph);
@@ -359,10 +416,19 @@ extern "C" int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* bu
         cudaGraphDestroy(graph);
         HYD_CUDA_TRY(ie);
         std::lock_guard<std::mutex> lock(g_graph_mu);
+        if (g_graphs.size() >= 64) {  // bounded cache: drop everything when full
+            for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
+            g_graphs.clear();
+        }
         g_graphs[key] = exec;
     }
     HYD_CUDA_TRY(cudaGraphLaunch(exec, st));
     return HYD_CUDA_OK;
+}
+
+extern "C" int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
+                                              int64_t iters, int* final_buf, void* stream) {
+    return hyd_cuda_iterate_stencil2d_f64_variant(kind, buf0, buf1, h, w, iters, -1, final_buf, stream);
 }
 
 extern "C" void hyd_cuda_stencil_release_graphs(void) {

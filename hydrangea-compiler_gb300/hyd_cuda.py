@@ -48,6 +48,14 @@ SIGNATURES = {
     "hyd_cuda_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _p]),
     "hyd_cuda_iterate_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _i64, C.POINTER(C.c_int), _p]),
     "hyd_cuda_stencil_release_graphs": (None, []),
+    "hyd_cuda_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i, _p]),
+    "hyd_cuda_iterate_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i64, _i, C.POINTER(C.c_int), _p]),
+    "hyd_cuda_tune_cache_path": (C.c_char_p, []),
+    "hyd_cuda_tune_set_cache_path": (_i, [C.c_char_p]),
+    "hyd_cuda_tune_record": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, _i, _d]),
+    "hyd_cuda_tune_query": (_i, [C.c_char_p, C.c_char_p, C.c_char_p]),
+    "hyd_cuda_autotune_stencil2d": (_i, [_i, _i64, _i64, _i, C.POINTER(C.c_int), _p]),
+    "hyd_cuda_autotune_histogram": (_i, [_i64, _i64, _i, C.POINTER(C.c_int), _p]),
     "hyd_cuda_scan_i64": (_i, [_p, _p, _i64, _i64, _i, _i, _p]),
     "hyd_cuda_scan_f64": (_i, [_p, _p, _i64, _d, _i, _i, _p]),
     "hyd_cuda_segmented_reduce_i64": (_i, [_p, _i64, _p, _i64, _i64, _p, _p]),
@@ -218,18 +226,37 @@ def scatter_add_f64(idx, vals, dst, stream=None):
          stream_handle(stream))
 
 
-def stencil2d(kind, src, dst, stream=None):
+STENCIL_VARIANTS = {0: (32, 32), 1: (16, 128), 2: (16, 64), 3: (32, 64), 4: (8, 128), 5: (32, 128), 6: "plain"}
+
+
+def stencil2d(kind, src, dst, stream=None, variant=-1):
     h, w = src.shape
-    call("hyd_cuda_stencil2d_f64", kind, ptr(src), ptr(dst), h, w, stream_handle(stream))
+    call("hyd_cuda_stencil2d_f64_variant", kind, ptr(src), ptr(dst), h, w, variant, stream_handle(stream))
 
 
-def iterate_stencil2d(kind, buf0, buf1, iters, stream=None):
+def iterate_stencil2d(kind, buf0, buf1, iters, stream=None, variant=-1):
     """Runs `iters` steps ping-ponging buf0/buf1; returns the buffer holding the result."""
     h, w = buf0.shape
     fb = C.c_int(-1)
-    call("hyd_cuda_iterate_stencil2d_f64", kind, ptr(buf0), ptr(buf1), h, w, iters, C.byref(fb),
-         stream_handle(stream))
+    call("hyd_cuda_iterate_stencil2d_f64_variant", kind, ptr(buf0), ptr(buf1), h, w, iters, variant,
+         C.byref(fb), stream_handle(stream))
     return buf0 if fb.value == 0 else buf1
+
+
+def autotune_stencil2d(kind, h, w, reps=5):
+    import numpy as np
+    best = C.c_int(-1)
+    times = np.zeros(7)
+    call("hyd_cuda_autotune_stencil2d", kind, h, w, reps, C.byref(best), times.ctypes.data)
+    return best.value, times
+
+
+def autotune_histogram(n, bins, reps=5):
+    import numpy as np
+    best = C.c_int(-1)
+    times = np.zeros(5)
+    call("hyd_cuda_autotune_histogram", n, bins, reps, C.byref(best), times.ctypes.data)
+    return best.value, times
 
 
 def scan(x, out, init=0, reverse=False, inclusive=False, stream=None):

@@ -159,6 +159,32 @@ int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t
                                    int64_t iters, int* final_buf, void* stream);
 /* Releases the cached iterate graphs (also done by hyd_cuda_cleanup). */
 void hyd_cuda_stencil_release_graphs(void);
+/* Same, with an explicit kernel variant instead of the autotuned one: 0..5 are
+ * TMA tile shapes (0 = 32x32, the reference's fixed polyhedral tile,
+ * Polyhedral.hs:196-204; 1 = 16x128, 2 = 16x64, 3 = 32x64, 4 = 8x128,
+ * 5 = 32x128), 6 = the plain non-TMA kernel, -1 = autotuned/default.  All
+ * variants give identical bits. */
+int hyd_cuda_stencil2d_f64_variant(int kind, const double* in, double* out, int64_t h, int64_t w,
+                                   int variant, void* stream);
+int hyd_cuda_iterate_stencil2d_f64_variant(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
+                                           int64_t iters, int variant, int* final_buf, void* stream);
+
+/* ---- autotuner ---------------------------------------------------------------
+ * Chooses, per (kernel, shape class), the fastest of candidates that all give
+ * identical results, measuring on the current device; choices persist in a
+ * tab-separated cache (HYD_CUDA_TUNE_CACHE, default
+ * $HOME/.cache/hydrangea_cuda_tune.tsv) and are consulted by AUTO launches.
+ * Shape classes: stencil2d "k<kind>_h<log2 h>_w<log2 w>", weighted_histogram
+ * "b<log2 bins>" (ceil log2). */
+const char* hyd_cuda_tune_cache_path(void);
+int hyd_cuda_tune_set_cache_path(const char* path);     /* reloads the table from `path` */
+int hyd_cuda_tune_record(const char* device, const char* kernel, const char* klass, int choice, double us);
+int hyd_cuda_tune_query(const char* device, const char* kernel, const char* klass);  /* -1 if absent */
+/* Time every stencil variant (times_us[7], may be NULL) / histogram strategy
+ * (times_us[5], index = strategy, -1 when it cannot run) on scratch inputs and
+ * record the fastest in *best. */
+int hyd_cuda_autotune_stencil2d(int kind, int64_t h, int64_t w, int reps, int* best, double* times_us);
+int hyd_cuda_autotune_histogram(int64_t n, int64_t bins, int reps, int* best, double* times_us);
 
 /* ---- scan family and segmented reduce ----------------------------------------
  * scan / scan_inclusive / scanr / scanr_inclusive with (+) and initial value

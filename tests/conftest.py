@@ -9,6 +9,11 @@ for p in (ROOT, PKG):
     if p not in sys.path:
         sys.path.insert(0, p)
 
+# keep the autotuner's on-disk cache of this test session out of $HOME
+if "HYD_CUDA_TUNE_CACHE" not in os.environ:
+    import tempfile
+    os.environ["HYD_CUDA_TUNE_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="hyd_tune_"), "tune.tsv")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
