@@ -30,6 +30,7 @@
 //    row's SpMV in the same warp.  Columns are unique within a row in this
 //    workload, so sorting fixes the in-row order and the CSR is bit-exact
 //    however the atomics interleaved.
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -331,8 +332,9 @@ __global__ void __launch_bounds__(kBatchThreads) batch_sort_spmv_kernel(
 // caller until the stream reaches this point) the tables are copied
 // asynchronously and the call returns without synchronizing; otherwise it
 // synchronizes the stream before returning.
-int batch_pipeline(std::vector<BatchInst>& inst, const char* key, cudaStream_t s, void* staging,
-                   size_t staging_bytes) {
+// Row-atomic form (see the file comment); the fallback of the bucketed form.
+int batch_pipeline_rows(std::vector<BatchInst>& inst, const char* key, cudaStream_t s, void* staging,
+                        size_t staging_bytes) {
     Device* d = nullptr;
     HYD_TRY(device(&d));
     std::vector<WorkItem> count_items, row_items;
@@ -403,8 +405,31 @@ int batch_pipeline(std::vector<BatchInst>& inst, const char* key, cudaStream_t s
     return HYD_CUDA_OK;
 }
 
-// Bytes of pinned staging batch_pipeline needs for `inst` (0 if none).
+int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStream_t s, void* staging,
+                            size_t staging_bytes);
+size_t batch_pipeline_bucketed_table_bytes(const std::vector<BatchInst>& bi);
+
+// The batched pipeline: the bucketed form (sparse_bucket.cu) when the batch is
+// within its limits, otherwise the row-atomic form.
+int batch_pipeline(std::vector<BatchInst>& inst, const char* key, cudaStream_t s, void* staging,
+                   size_t staging_bytes) {
+    const char* force = getenv("HYD_CUDA_BATCH_PIPELINE");  // "rows" forces the row-atomic form
+    if (!(force && strcmp(force, "rows") == 0)) {
+        const int st = batch_pipeline_bucketed(inst, key, s, staging, staging_bytes);
+        if (st != HYD_CUDA_ERR_UNSUPPORTED) return st;
+    }
+    return batch_pipeline_rows(inst, key, s, staging, staging_bytes);
+}
+
+static size_t batch_pipeline_rows_table_bytes(const std::vector<BatchInst>& inst);
+
+// Bytes of pinned staging batch_pipeline needs for `inst`.
 size_t batch_pipeline_table_bytes(const std::vector<BatchInst>& inst) {
+    const size_t a = batch_pipeline_bucketed_table_bytes(inst), b = batch_pipeline_rows_table_bytes(inst);
+    return a > b ? a : b;
+}
+
+static size_t batch_pipeline_rows_table_bytes(const std::vector<BatchInst>& inst) {
     size_t ci = 0, ri = 0;
     for (const BatchInst& I : inst) {
         ci += (size_t)((I.nnz + kEntryTile - 1) / kEntryTile);

@@ -1,0 +1,511 @@
+// sparse_bucket.cu -- the batched COO -> CSR -> SpMV pipeline, bucketed form.
+//
+// Same contract as batch_pipeline in sparse.cu (per instance: CSR of the
+// entries sorted by (row, col), y = A x), organised so that no stage walks
+// rows one dependent memory chain at a time:
+//  1. count   per (instance, 8192-entry tile): a shared-memory histogram of
+//             64-row buckets (row >> 6), flushed with one global red per
+//             non-empty bucket;
+//  2. scan    exclusive scan of the ~4e5 bucket counts gives every bucket's
+//             first slot (instances are contiguous, so bucket starts are also
+//             each instance's entry offsets);
+//  3. split   per tile again: each entry gets its rank inside (tile, bucket)
+//             from a shared-memory atomic, each (tile, bucket) reserves its run
+//             with one global atomic, and the entry is written to the bucket's
+//             region as a 32-bit key (row_in_bucket << 24 | col) plus its value;
+//  4. bucket  one CTA per bucket: its entries (at most 2048 in the fast kernel)
+//             are counting-sorted by row into shared memory (64 counters), then
+//             each warp takes rows, sorts a row by column in registers (bitonic
+//             network over shuffles), writes its CSR columns/values and computes
+//             its SpMV; the row pointers are the shared row offsets.  Buckets
+//             above 2048 entries (64 rows x at most 256) go to an overflow list
+//             handled by a block-wide bitonic sort in 96 KB of shared memory.
+// Requires ncols < 2^24 (24-bit column field) and at most 256 entries per row.
+#include <cstring>
+#include <vector>
+
+#include "batch.cuh"
+#include "hyd_common.cuh"
+
+namespace hyd {
+
+int scan_i64_launch(const long long* in, long long* out, int64_t n, long long init, bool reverse,
+                    bool inclusive, cudaStream_t stream);
+
+constexpr int kBkThreads = 512;
+constexpr int kBkShift = 6;                  // 64 rows per bucket
+constexpr int kBkRows = 1 << kBkShift;
+constexpr int kBkCap = kBkRows * 256;        // entries per bucket at most (256 per row)
+constexpr int kTileEntries = 8192;           // entries per count/split work item
+constexpr int kMaxSmemBuckets = 4096;        // per instance (2^18 rows)
+
+struct BkInst {
+    long long nrows, ncols, nnz;
+    long long bucket_base;  // first bucket in the batch-wide bucket space
+    long long nbuckets;
+    long long scan_base;    // entries of all earlier instances
+    const int* rows;
+    const int* cols;
+    const double* vals;
+    const double* x;
+    long long* row_ptr;
+    int* csr_cols;
+    double* csr_vals;
+    double* y;
+};
+
+struct BkItem {
+    int inst;
+    int tile;  // entry tile (stages 1, 3) or bucket index (stage 4)
+};
+
+__device__ __forceinline__ bool bk_next(unsigned* cursor, unsigned nitems, unsigned& item) {
+    __shared__ unsigned sh_item;
+    if (threadIdx.x == 0) sh_item = atomicAdd(cursor, 1u);
+    __syncthreads();
+    item = sh_item;
+    __syncthreads();
+    return item < nitems;
+}
+
+// Stage 1.
+__global__ void __launch_bounds__(kBkThreads) bk_count_kernel(const BkInst* __restrict__ inst,
+                                                              const BkItem* __restrict__ items, unsigned nitems,
+                                                              unsigned* cursor, unsigned* __restrict__ bcount,
+                                                              unsigned* err) {
+    __shared__ unsigned hist[kMaxSmemBuckets];
+    unsigned it;
+    bool bad = false;
+    while (bk_next(cursor, nitems, it)) {
+        const BkItem w = items[it];
+        const BkInst I = inst[w.inst];
+        const bool smem = I.nbuckets <= kMaxSmemBuckets;
+        if (smem)
+            for (int b = threadIdx.x; b < I.nbuckets; b += kBkThreads) hist[b] = 0u;
+        __syncthreads();
+        const long long t0 = (long long)w.tile * kTileEntries;
+        const long long t1 = t0 + kTileEntries < I.nnz ? t0 + kTileEntries : I.nnz;
+        for (long long k = t0 + threadIdx.x; k < t1; k += kBkThreads) {
+            const int r = I.rows[k], c = I.cols[k];
+            if (r < 0 || r >= I.nrows || c < 0 || c >= I.ncols) {
+                bad = true;
+                continue;
+            }
+            if (smem) atomicAdd(&hist[r >> kBkShift], 1u);
+            else atomicAdd(&bcount[I.bucket_base + (r >> kBkShift)], 1u);
+        }
+        __syncthreads();
+        if (smem)
+            for (int b = threadIdx.x; b < I.nbuckets; b += kBkThreads)
+                if (hist[b]) atomicAdd(&bcount[I.bucket_base + b], hist[b]);
+        __syncthreads();
+    }
+    if (bad) raise_error(err, ERRBIT_BOUNDS);
+}
+
+__global__ void bk_widen_kernel(const unsigned* __restrict__ c, long long* __restrict__ out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = c[i];
+}
+
+// Stage 3.
+constexpr int kSplitPer = kTileEntries / kBkThreads;  // 16 entries per thread
+__global__ void __launch_bounds__(kBkThreads) bk_split_kernel(const BkInst* __restrict__ inst,
+                                                              const BkItem* __restrict__ items, unsigned nitems,
+                                                              unsigned* cursor, const long long* __restrict__ bstart,
+                                                              unsigned* __restrict__ bfill,
+                                                              unsigned* __restrict__ keys_out,
+                                                              double* __restrict__ vals_out) {
+    __shared__ unsigned hist[kMaxSmemBuckets];
+    __shared__ unsigned gbase[kMaxSmemBuckets];  // batch-wide slots (< 2^32, checked on the host)
+    unsigned it;
+    while (bk_next(cursor, nitems, it)) {
+        const BkItem w = items[it];
+        const BkInst I = inst[w.inst];
+        const bool smem = I.nbuckets <= kMaxSmemBuckets;
+        if (smem)
+            for (int b = threadIdx.x; b < I.nbuckets; b += kBkThreads) hist[b] = 0u;
+        __syncthreads();
+        const long long t0 = (long long)w.tile * kTileEntries;
+        const long long t1 = t0 + kTileEntries < I.nnz ? t0 + kTileEntries : I.nnz;
+        unsigned key[kSplitPer], rank[kSplitPer];
+        int bucket[kSplitPer];
+#pragma unroll
+        for (int j = 0; j < kSplitPer; ++j) {
+            const long long k = t0 + threadIdx.x + (long long)j * kBkThreads;
+            bucket[j] = -1;
+            if (k < t1) {
+                const int r = I.rows[k], c = I.cols[k];
+                if (r >= 0 && r < I.nrows && c >= 0 && c < I.ncols) {  // invalid ones were reported by stage 1
+                    bucket[j] = r >> kBkShift;
+                    key[j] = ((unsigned)(r & (kBkRows - 1)) << 24) | (unsigned)c;
+                    if (smem) rank[j] = atomicAdd(&hist[bucket[j]], 1u);
+                }
+            }
+        }
+        __syncthreads();
+        if (smem) {
+            for (int b = threadIdx.x; b < I.nbuckets; b += kBkThreads) {
+                const unsigned c = hist[b];
+                gbase[b] = c ? (unsigned)(bstart[I.bucket_base + b] + atomicAdd(&bfill[I.bucket_base + b], c)) : 0u;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kSplitPer; ++j) {
+            if (bucket[j] < 0) continue;
+            const long long k = t0 + threadIdx.x + (long long)j * kBkThreads;
+            const long long pos = smem ? (long long)gbase[bucket[j]] + rank[j]
+                                       : bstart[I.bucket_base + bucket[j]] +
+                                             atomicAdd(&bfill[I.bucket_base + bucket[j]], 1u);
+            keys_out[pos] = key[j];
+            vals_out[pos] = I.vals[k];
+        }
+        __syncthreads();
+    }
+}
+
+// ---- stage 4 ------------------------------------------------------------------
+constexpr int kBkSmallThreads = 256;
+constexpr int kBkSmallWarps = kBkSmallThreads / 32;
+constexpr int kBkSmallCap = 2048;  // entries of a bucket handled in the fast kernel
+constexpr int kBkRounds = kBkSmallCap / kBkSmallThreads;  // 32-element rounds per warp
+// two (key, index) buffers, per-(warp, digit) counts, digit bases
+constexpr size_t kBkSmallSmem = (size_t)kBkSmallCap * 12 + (size_t)kBkSmallWarps * 256 * 4 + 256 * 4;
+
+// Fast path: a stable LSD radix sort of the bucket's keys (row << 24 | col) in
+// shared memory, 8-bit digits over the column bits then one pass on the row
+// digit; each warp owns 256 consecutive positions, ranked in rounds of 32 with
+// __match_any_sync so equal digits keep their order.  The last pass's digit
+// bases are the row offsets.  Then CSR columns/values are written in sorted
+// order (values gathered by index), and each warp computes the SpMV of its
+// rows with lane i summing sorted positions i, i+32, ... (the same order as the
+// other kernels).  Buckets above kBkSmallCap go to `overflow`.
+__global__ void __launch_bounds__(kBkSmallThreads) bk_bucket_small_kernel(
+    const BkInst* __restrict__ inst, const BkItem* __restrict__ items, unsigned nitems, unsigned* cursor,
+    const long long* __restrict__ bstart, const unsigned* __restrict__ bcount, const unsigned* __restrict__ keys_in,
+    const double* __restrict__ vals_in, BkItem* __restrict__ overflow, unsigned* overflow_count, unsigned* err) {
+    extern __shared__ __align__(16) unsigned char bks_smem[];
+    unsigned* kbuf0 = reinterpret_cast<unsigned*>(bks_smem);
+    unsigned* kbuf1 = kbuf0 + kBkSmallCap;
+    unsigned short* ibuf0 = reinterpret_cast<unsigned short*>(kbuf1 + kBkSmallCap);
+    unsigned short* ibuf1 = ibuf0 + kBkSmallCap;
+    unsigned* wcount = reinterpret_cast<unsigned*>(ibuf1 + kBkSmallCap);  // [warps][256]
+    unsigned* dbase = wcount + kBkSmallWarps * 256;                        // [256]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    unsigned it;
+    bool bad = false;
+    while (bk_next(cursor, nitems, it)) {
+        const BkItem w = items[it];
+        const BkInst I = inst[w.inst];
+        const long long gb = I.bucket_base + w.tile;
+        const int E = (int)bcount[gb];
+        if (E > kBkSmallCap) {
+            if (threadIdx.x == 0) overflow[atomicAdd(overflow_count, 1u)] = w;
+            continue;  // uniform
+        }
+        const long long s0 = bstart[gb];
+        const long long e0 = s0 - I.scan_base;
+        const long long r0 = (long long)w.tile << kBkShift;
+        const int nr = (int)((I.nrows - r0) < kBkRows ? (I.nrows - r0) : kBkRows);
+        for (int i = threadIdx.x; i < E; i += kBkSmallThreads) {
+            kbuf0[i] = keys_in[s0 + i];
+            ibuf0[i] = (unsigned short)i;
+        }
+        // positions split evenly over the warps (whole 32-element rounds); warp
+        // order is position order, so ranks stay stable
+        const int chunk = (((E + kBkSmallWarps - 1) / kBkSmallWarps) + 31) & ~31;
+        const int rounds = chunk / 32;
+        int cbits = 0;
+        while ((1LL << cbits) < I.ncols) ++cbits;
+        const int col_passes = (cbits + 7) / 8;
+        unsigned* kin = kbuf0;
+        unsigned* kout = kbuf1;
+        unsigned short* iin = ibuf0;
+        unsigned short* iout = ibuf1;
+        __syncthreads();
+        for (int pass = 0; pass <= col_passes; ++pass) {
+            const int shift = pass < col_passes ? 8 * pass : 24;  // last pass: the row digit
+            for (int i = threadIdx.x; i < kBkSmallWarps * 256; i += kBkSmallThreads) wcount[i] = 0u;
+            __syncthreads();
+            unsigned rk[kBkRounds];
+            unsigned dg[kBkRounds];
+#pragma unroll
+            for (int r = 0; r < kBkRounds; ++r) {
+                if (r >= rounds) break;  // warp-uniform
+                const int pos = warp * chunk + r * 32 + lane;
+                const bool ok = pos < E && pos < (warp + 1) * chunk;
+                const unsigned d = ok ? ((kin[pos] >> shift) & 0xFFu) : 0x100u;
+                dg[r] = d;
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                unsigned prior = 0;
+                if (ok) prior = wcount[warp * 256 + d];
+                __syncwarp();
+                rk[r] = prior + __popc(peers & lt);
+                if (ok && (peers & lt) == 0u) wcount[warp * 256 + d] = prior + __popc(peers);
+                __syncwarp();
+            }
+            __syncthreads();
+            // digit totals, their exclusive scan, then per-(warp, digit) bases
+            const int dgt = threadIdx.x;  // 256 threads <-> 256 digits
+            unsigned tot = 0;
+#pragma unroll
+            for (int ww = 0; ww < kBkSmallWarps; ++ww) tot += wcount[ww * 256 + dgt];
+            unsigned incl = tot;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += y;
+            }
+            if (lane == 31) dbase[warp] = incl;
+            __syncthreads();
+            unsigned wpre = 0;
+            for (int ww = 0; ww < warp; ++ww) wpre += dbase[ww];
+            __syncthreads();
+            unsigned run = wpre + incl - tot;  // exclusive base of digit dgt
+            dbase[dgt] = run;
+#pragma unroll
+            for (int ww = 0; ww < kBkSmallWarps; ++ww) {
+                const unsigned c = wcount[ww * 256 + dgt];
+                wcount[ww * 256 + dgt] = run;
+                run += c;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kBkRounds; ++r) {
+                if (r >= rounds) break;
+                const int pos = warp * chunk + r * 32 + lane;
+                if (pos < E && pos < (warp + 1) * chunk) {
+                    const unsigned dst = wcount[warp * 256 + dg[r]] + rk[r];
+                    kout[dst] = kin[pos];
+                    iout[dst] = iin[pos];
+                }
+            }
+            __syncthreads();
+            unsigned* tk = kin; kin = kout; kout = tk;
+            unsigned short* ti = iin; iin = iout; iout = ti;
+        }
+        // kin/iin: sorted by (row, col); dbase[r] = first position of row r
+        for (int p = threadIdx.x; p < E; p += kBkSmallThreads) {
+            I.csr_cols[e0 + p] = (int)(kin[p] & 0xFFFFFFu);
+            I.csr_vals[e0 + p] = vals_in[s0 + iin[p]];
+        }
+        for (int r = threadIdx.x; r <= nr; r += kBkSmallThreads) {
+            if (r < nr) I.row_ptr[r0 + r] = e0 + dbase[r];
+            else if (r0 + nr == I.nrows) I.row_ptr[I.nrows] = I.nnz;
+        }
+        for (int r = warp; r < nr; r += kBkSmallWarps) {
+            const int a = (int)dbase[r], b = r + 1 < kBkRows ? (int)dbase[r + 1] : E;
+            const int bb = r + 1 < nr ? b : E;
+            if (bb - a > 256) bad = true;  // a row above 256 entries: outside the contract
+            double acc = 0.0;
+            for (int p = a + lane; p < bb; p += 32)
+                acc = fma(vals_in[s0 + iin[p]], I.x[kin[p] & 0xFFFFFFu], acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) I.y[r0 + r] = acc;
+        }
+        __syncthreads();
+    }
+    if (bad) raise_error(err, ERRBIT_BOUNDS);
+}
+
+// Large buckets (up to 64 rows x 256): one CTA sorts the bucket's keys with a
+// block-wide bitonic network in shared memory.  Reads its item count from
+// device memory (filled by the fast kernel).
+constexpr size_t kBkSmem = (size_t)kBkCap * 6 + 1024;
+
+__global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __restrict__ inst,
+                                                               const BkItem* __restrict__ items,
+                                                               const unsigned* nitems_dev, unsigned* cursor,
+                                                               const long long* __restrict__ bstart,
+                                                               const unsigned* __restrict__ bcount,
+                                                               const unsigned* __restrict__ keys_in,
+                                                               const double* __restrict__ vals_in, unsigned* err) {
+    extern __shared__ __align__(16) unsigned char bk_smem[];
+    unsigned* key = reinterpret_cast<unsigned*>(bk_smem);
+    unsigned short* idx = reinterpret_cast<unsigned short*>(bk_smem + (size_t)kBkCap * 4);
+    __shared__ int rstart[kBkRows + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned nitems = *nitems_dev;
+    unsigned it;
+    bool bad = false;
+    while (bk_next(cursor, nitems, it)) {
+        const BkItem w = items[it];
+        const BkInst I = inst[w.inst];
+        const long long gb = I.bucket_base + w.tile;
+        const int E = (int)bcount[gb];
+        const long long s0 = bstart[gb];        // batch-wide slot of the bucket's first entry
+        const long long e0 = s0 - I.scan_base;  // instance-relative
+        const long long r0 = (long long)w.tile << kBkShift;
+        const int nr = (int)((I.nrows - r0) < kBkRows ? (I.nrows - r0) : kBkRows);
+        if (E > kBkCap) {  // a row above 256 entries: outside the contract
+            bad = true;
+            continue;
+        }
+        int P = 1;
+        while (P < E) P <<= 1;
+        for (int i = threadIdx.x; i < P; i += kBkThreads) {
+            key[i] = i < E ? keys_in[s0 + i] : 0xFFFFFFFFu;
+            idx[i] = (unsigned short)i;
+        }
+        __syncthreads();
+        for (int size = 2; size <= P; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = threadIdx.x; i < P / 2; i += kBkThreads) {
+                    const int lo = 2 * i - (i & (stride - 1));
+                    const int hi = lo + stride;
+                    const bool up = (lo & size) == 0;
+                    const unsigned a = key[lo], b = key[hi];
+                    if ((a > b) == up) {
+                        key[lo] = b;
+                        key[hi] = a;
+                        const unsigned short t = idx[lo];
+                        idx[lo] = idx[hi];
+                        idx[hi] = t;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int p = threadIdx.x; p <= E; p += kBkThreads) {
+            const int rp = p == 0 ? -1 : (int)(key[p - 1] >> 24);
+            const int rc = p == E ? nr : (int)(key[p] >> 24);
+            for (int r = rp + 1; r <= rc && r <= nr; ++r) rstart[r] = p;
+        }
+        __syncthreads();
+        for (int p = threadIdx.x; p < E; p += kBkThreads) {
+            I.csr_cols[e0 + p] = (int)(key[p] & 0xFFFFFFu);
+            I.csr_vals[e0 + p] = vals_in[s0 + idx[p]];
+        }
+        for (int r = threadIdx.x; r <= nr; r += kBkThreads) {
+            if (r < nr) I.row_ptr[r0 + r] = e0 + rstart[r];
+            else if (r0 + nr == I.nrows) I.row_ptr[I.nrows] = I.nnz;
+        }
+        for (int r = warp; r < nr; r += kBkThreads / 32) {
+            double acc = 0.0;
+            for (int p = rstart[r] + lane; p < rstart[r + 1]; p += 32)
+                acc = fma(vals_in[s0 + idx[p]], I.x[key[p] & 0xFFFFFFu], acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) I.y[r0 + r] = acc;
+        }
+        __syncthreads();
+    }
+    if (bad) raise_error(err, ERRBIT_BOUNDS);
+}
+
+// Bucketed pipeline; returns HYD_CUDA_ERR_UNSUPPORTED (nothing launched) when a
+// batch falls outside its limits so the caller can take the row-atomic path.
+int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStream_t s, void* staging,
+                            size_t staging_bytes) {
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    std::vector<BkInst> inst(bi.size());
+    std::vector<BkItem> tiles, buckets;
+    long long nb_total = 0, entries = 0;
+    for (size_t i = 0; i < bi.size(); ++i) {
+        const BatchInst& B = bi[i];
+        if (B.ncols >= (1LL << 24) || B.nrows >= (1LL << 31)) return HYD_CUDA_ERR_UNSUPPORTED;
+        BkInst& I = inst[i];
+        I.nrows = B.nrows;
+        I.ncols = B.ncols;
+        I.nnz = B.nnz;
+        I.nbuckets = (B.nrows + kBkRows - 1) / kBkRows;
+        I.bucket_base = nb_total;
+        I.scan_base = entries;
+        I.rows = B.rows;
+        I.cols = B.cols;
+        I.vals = B.vals;
+        I.x = B.x;
+        I.row_ptr = B.row_ptr;
+        I.csr_cols = B.csr_cols;
+        I.csr_vals = B.csr_vals;
+        I.y = B.y;
+        for (long long t = 0; t * kTileEntries < B.nnz; ++t) tiles.push_back(BkItem{(int)i, (int)t});
+        for (long long b = 0; b < I.nbuckets; ++b) buckets.push_back(BkItem{(int)i, (int)b});
+        nb_total += I.nbuckets;
+        entries += B.nnz;
+    }
+    if (nb_total >= (1LL << 31) || entries >= (1LL << 32)) return HYD_CUDA_ERR_UNSUPPORTED;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t inst_b = al(inst.size() * sizeof(BkInst)), tiles_b = al(tiles.size() * sizeof(BkItem)),
+                 bk_b = al(buckets.size() * sizeof(BkItem));
+    const size_t cnt_b = al((size_t)nb_total * 4), wide_b = al((size_t)nb_total * 8);
+    const size_t keys_b = al((size_t)entries * 4), vals_b = al((size_t)entries * 8);
+    void* buf = nullptr;
+    HYD_TRY(device_buffer(d, key, inst_b + tiles_b + 2 * bk_b + 2 * cnt_b + 2 * wide_b + keys_b + vals_b + 256, &buf));
+    unsigned char* b = static_cast<unsigned char*>(buf);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char* p = b + off;
+        off += bytes;
+        return p;
+    };
+    BkInst* d_inst = reinterpret_cast<BkInst*>(take(inst_b));
+    BkItem* d_tiles = reinterpret_cast<BkItem*>(take(tiles_b));
+    BkItem* d_bk = reinterpret_cast<BkItem*>(take(bk_b));
+    unsigned* bcount = reinterpret_cast<unsigned*>(take(cnt_b));
+    unsigned* bfill = reinterpret_cast<unsigned*>(take(cnt_b));
+    long long* wide = reinterpret_cast<long long*>(take(wide_b));
+    long long* bstart = reinterpret_cast<long long*>(take(wide_b));
+    unsigned* keys = reinterpret_cast<unsigned*>(take(keys_b));
+    double* vals = reinterpret_cast<double*>(take(vals_b));
+    BkItem* overflow = reinterpret_cast<BkItem*>(take(bk_b));
+    unsigned* cursors = reinterpret_cast<unsigned*>(take(256));
+    const size_t table = inst_b + tiles_b + bk_b;
+    const bool async_tables = staging != nullptr && staging_bytes >= table;
+    if (async_tables) {
+        unsigned char* h = static_cast<unsigned char*>(staging);
+        memcpy(h, inst.data(), inst.size() * sizeof(BkInst));
+        if (!tiles.empty()) memcpy(h + inst_b, tiles.data(), tiles.size() * sizeof(BkItem));
+        memcpy(h + inst_b + tiles_b, buckets.data(), buckets.size() * sizeof(BkItem));
+        HYD_CUDA_TRY(cudaMemcpyAsync(b, h, table, cudaMemcpyHostToDevice, s));
+    } else {
+        HYD_CUDA_TRY(cudaMemcpyAsync(d_inst, inst.data(), inst.size() * sizeof(BkInst), cudaMemcpyHostToDevice, s));
+        if (!tiles.empty())
+            HYD_CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(BkItem), cudaMemcpyHostToDevice, s));
+        HYD_CUDA_TRY(cudaMemcpyAsync(d_bk, buckets.data(), buckets.size() * sizeof(BkItem), cudaMemcpyHostToDevice, s));
+    }
+    HYD_CUDA_TRY(cudaMemsetAsync(bcount, 0, 2 * cnt_b, s));  // bcount and bfill
+    HYD_CUDA_TRY(cudaMemsetAsync(cursors, 0, 64, s));
+    const unsigned grid = (unsigned)(d->sm_count * 2);
+    if (!tiles.empty()) {
+        bk_count_kernel<<<grid, kBkThreads, 0, s>>>(d_inst, d_tiles, (unsigned)tiles.size(), cursors + 0, bcount,
+                                                    d->d_err);
+        HYD_TRY(launch_check("bk_count"));
+    }
+    bk_widen_kernel<<<grid, 256, 0, s>>>(bcount, wide, nb_total);
+    HYD_TRY(launch_check("bk_widen"));
+    HYD_TRY(scan_i64_launch(wide, bstart, nb_total, 0, false, false, s));
+    if (!tiles.empty()) {
+        bk_split_kernel<<<grid, kBkThreads, 0, s>>>(d_inst, d_tiles, (unsigned)tiles.size(), cursors + 1, bstart,
+                                                    bfill, keys, vals);
+        HYD_TRY(launch_check("bk_split"));
+    }
+    HYD_TRY(configure_kernel((const void*)bk_bucket_small_kernel, d, false));
+    bk_bucket_small_kernel<<<(unsigned)(d->sm_count * 4), kBkSmallThreads, kBkSmallSmem, s>>>(
+        d_inst, d_bk, (unsigned)buckets.size(), cursors + 2, bstart, bcount, keys, vals, overflow, cursors + 4,
+        d->d_err);
+    HYD_TRY(launch_check("bk_bucket_small"));
+    HYD_TRY(configure_kernel((const void*)bk_bucket_kernel, d, false));
+    bk_bucket_kernel<<<grid, kBkThreads, kBkSmem, s>>>(d_inst, overflow, cursors + 4, cursors + 3, bstart, bcount,
+                                                       keys, vals, d->d_err);
+    HYD_TRY(launch_check("bk_bucket_large"));
+    if (!async_tables) HYD_CUDA_TRY(cudaStreamSynchronize(s));
+    return HYD_CUDA_OK;
+}
+
+size_t batch_pipeline_bucketed_table_bytes(const std::vector<BatchInst>& bi) {
+    size_t tiles = 0, buckets = 0;
+    for (const BatchInst& B : bi) {
+        tiles += (size_t)((B.nnz + kTileEntries - 1) / kTileEntries);
+        buckets += (size_t)((B.nrows + kBkRows - 1) / kBkRows);
+    }
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    return al(bi.size() * sizeof(BkInst)) + al(tiles * sizeof(BkItem)) + al(buckets * sizeof(BkItem));
+}
+
+}  // namespace hyd

@@ -148,3 +148,16 @@ def test_batched_workload_instances_subset(hc, orc, dev):
     out = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
     hc.check(hc.device_check())
     _check_batch(hc, orc, desc, rows, cols, vals, x, *out)
+
+
+def test_bucketed_and_row_atomic_forms_agree(hc, orc, dev, monkeypatch):
+    """Both internal forms of the batched pipeline give identical CSR and y."""
+    desc, rows, cols, vals, x = hc.synth_coo_batch(12, seed0=321, min_log2=10, max_log2=15)
+    monkeypatch.setenv("HYD_CUDA_BATCH_PIPELINE", "rows")
+    a = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
+    monkeypatch.delenv("HYD_CUDA_BATCH_PIPELINE")
+    b = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
+    hc.check(hc.device_check())
+    for u, v in zip(a, b):
+        assert torch.equal(u, v)
+    _check_batch(hc, orc, desc, rows, cols, vals, x, *b)
