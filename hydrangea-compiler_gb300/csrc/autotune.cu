@@ -253,7 +253,7 @@ int hyd_cuda_autotune_histogram(int64_t n, int64_t bins, int reps, int* best, do
     int st = hyd_cuda_fill_uniform_i64(data, n, 2, 1LL << 20, s);
     double best_us = 1e300;
     int best_v = -1;
-    for (int v = HYD_SCATTER_SMEM_WARP; v <= HYD_SCATTER_GLOBAL && st == HYD_CUDA_OK; ++v) {
+    for (int v = HYD_SCATTER_SMEM_WARP; v <= HYD_SCATTER_PARTITION && st == HYD_CUDA_OK; ++v) {
         double us = 0.0;
         const int r = time_us([&] { return hyd_cuda_weighted_histogram_i64(data, n, bins, hist, v, s); }, reps, s, &us);
         if (times_us) times_us[v] = r == HYD_CUDA_OK ? us : -1.0;

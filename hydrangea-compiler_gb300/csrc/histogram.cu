@@ -48,6 +48,9 @@ struct WeightedHistSourceT {
     const int64_t* data;
     DivMod64 dm;
     static constexpr bool kPackable = true;  // one 64-bit word per element
+    // the bin of a non-negative x is its low word masked (bins <= 2^31)
+    static constexpr bool kMaskRoute = kPow2;
+    __device__ __forceinline__ unsigned mask32() const { return (unsigned)dm.mask; }
     // Branch-free for a power of two: the masked value is the bin of every
     // non-negative x; a negative x has C remainder -((-x) & mask), which is in
     // range only when it is 0, i.e. exactly when x & mask == 0.  An out-of-range
@@ -97,6 +100,8 @@ struct ScatterI64Source {
     const int64_t* idx;
     const int64_t* vals;
     static constexpr bool kPackable = false;
+    static constexpr bool kMaskRoute = false;
+    __device__ __forceinline__ unsigned mask32() const { return 0u; }
     __device__ __forceinline__ void one(int64_t i, long long& bin, u64& val) const {
         bin = idx[i];
         val = (u64)vals[i];
@@ -438,6 +443,384 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     if (bad) raise_error(err, ERRBIT_BOUNDS);
 }
 
+// ---- partition: a staging pass, then one shared-memory pass per bin range -----
+// For bins beyond one SM's shared memory.  Pass 1 reads the data once and
+// writes every tile of kPartTile elements back, in place in a staging buffer,
+// with its elements grouped by bin range (range = bin >> kPartShift) and the
+// P + 1 run boundaries of the tile in a table.  Pass 2 is a persistent kernel
+// over (range, chunk of tiles) work items taken in range order: a CTA keeps
+// the 2^kPartShift bins of its current range as 32-bit limbs in shared memory,
+// reads only that range's run of each tile, and flushes the limbs to the
+// histogram with global atomics when it moves to another range.  Per element:
+// one word read, written and read again, and shared-memory atomics, instead
+// of one L2 atomic.  Integer sums are exact, so the order inside a run is
+// immaterial.
+constexpr int kPartThreads = 512;
+constexpr int kPartEPT = 8;
+constexpr int kPartTile = kPartThreads * kPartEPT;  // 4096 elements
+constexpr int kPartWarps = kPartThreads / 32;
+constexpr int kPartMaxRanges = 32;
+constexpr int kPartShift = 14;  // 16384 bins (128 KB of limbs) per range
+// three tile buffers (bulk-loaded, grouped in place, bulk-stored) + mbarriers
+constexpr int kPartBufs = 3;
+constexpr size_t kPartStageSmem = kPartBufs * (size_t)kPartTile * 8 + 8 * kPartBufs;
+constexpr int kApplyThreads = 1024;
+constexpr int kApplyUnroll = 8;
+constexpr int64_t kPartMaxStage = (int64_t)1 << 27;  // elements staged per round
+constexpr int64_t kPartAutoMin = (int64_t)1 << 23;   // AUTO picks the partition from here
+// queue words after the stream's counter base: [0] finished apply CTAs,
+// [32 + r] elements of range r; the last apply CTA to finish zeroes them for
+// the next round
+constexpr int kPartQueueWord = 64;
+
+// Pass 1.  Tiles stream through three shared-memory buffers: one thread
+// bulk-loads tile i + 2 while tile i is grouped (mbarrier completion, bounded
+// waits), and the grouped tile is bulk-stored from the same buffer.  Every
+// thread counts its eight elements per range in packed 16-bit fields (NW words
+// of two ranges); one block-wide exclusive scan of those words gives each
+// thread its offset inside every range; the elements, held in registers, are
+// then written back into the buffer they were read from in range order.
+template <class Src, int NW>
+__global__ void __launch_bounds__(kPartThreads, 2)
+    hist_part_stage_kernel(Src src, const int64_t n, const bool bulk, const long long bins, const int P,
+                           const int64_t ntiles, u64* __restrict__ staged, unsigned short* __restrict__ bounds,
+                           unsigned* __restrict__ counts, unsigned* err) {
+    extern __shared__ __align__(128) unsigned char part_smem[];
+    u64* inbuf = reinterpret_cast<u64*>(part_smem);
+    const unsigned in0 = (unsigned)__cvta_generic_to_shared(inbuf);
+    const unsigned bar0 = in0 + kPartBufs * kPartTile * 8;
+    __shared__ unsigned wtot[NW][kPartWarps];
+    __shared__ unsigned rstart[kPartMaxRanges + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    bool bad = false;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < kPartBufs; ++q) mbar_init(bar0 + 8 * q, 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    // bytes of tile t that come in bulk: its whole 16-byte units
+    auto bulk_bytes = [&](int64_t t) -> unsigned {
+        const int64_t cnt = n - t * kPartTile < kPartTile ? n - t * kPartTile : kPartTile;
+        return bulk ? (unsigned)((cnt * 8) & ~(int64_t)15) : 0u;
+    };
+    auto issue = [&](int64_t t, int buf) {
+        const unsigned bytes = bulk_bytes(t);
+        mbar_expect_tx(bar0 + 8 * buf, bytes);
+        if (bytes) bulk_load_1d(in0 + buf * kPartTile * 8, src.data + t * kPartTile, bytes, bar0 + 8 * buf);
+    };
+    if (threadIdx.x == 0)
+        for (int q = 0; q < kPartBufs - 1; ++q)
+            if (blockIdx.x + (int64_t)q * gridDim.x < ntiles) issue(blockIdx.x + (int64_t)q * gridDim.x, q);
+    int64_t tile = blockIdx.x;
+    unsigned it = 0;
+    bool timed_out = false;
+    for (; tile < ntiles; tile += gridDim.x, ++it) {
+        const int buf = (int)(it % kPartBufs);
+        const int64_t ahead = tile + (int64_t)(kPartBufs - 1) * gridDim.x;
+        if (threadIdx.x == 0 && ahead < ntiles) {
+            // the buffer of tile i - 1: its bulk store must have read it
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(ahead, (int)((it + kPartBufs - 1) % kPartBufs));
+        }
+        const bool arrived = mbar_wait_bounded(bar0 + 8 * buf, (it / kPartBufs) & 1u);
+        if (__syncthreads_or(!arrived)) {
+            timed_out = true;
+            break;
+        }
+        const int64_t e0 = tile * kPartTile;
+        const int cnt = (int)(n - e0 < kPartTile ? n - e0 : kPartTile);
+        const int have = (int)(bulk_bytes(tile) / 8);
+        u64* const in = inbuf + buf * kPartTile;
+        u64 x[kPartEPT];
+        int r[kPartEPT];  // range; -1: no element or out of range
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j0 = 4 * (threadIdx.x + h * kPartThreads);
+            if (j0 + 4 <= have) {
+                const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(in + j0);
+                const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(in + j0 + 2);
+                x[4 * h] = a.x; x[4 * h + 1] = a.y; x[4 * h + 2] = b.x; x[4 * h + 3] = b.y;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) r[4 * h + q] = 0;
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int j = j0 + q;
+                    r[4 * h + q] = j < cnt ? 0 : -1;
+                    x[4 * h + q] = j < have ? in[j] : (j < cnt ? src.raw1(e0 + j) : 0ULL);
+                }
+            }
+        }
+        bool fast = false;
+        if constexpr (Src::kMaskRoute) {
+            // all present elements non-negative: the bin is the masked low word
+            unsigned hi_or = 0u;
+#pragma unroll
+            for (int k = 0; k < kPartEPT; ++k) hi_or |= r[k] == 0 ? (unsigned)(x[k] >> 32) : 0u;
+            if ((int)hi_or >= 0) {
+                fast = true;
+                const unsigned m = src.mask32();
+#pragma unroll
+                for (int k = 0; k < kPartEPT; ++k)
+                    if (r[k] == 0) r[k] = (int)(((unsigned)x[k] & m) >> kPartShift);
+            }
+        }
+        if (!fast) {
+#pragma unroll
+            for (int k = 0; k < kPartEPT; ++k) {
+                if (r[k] == 0) {
+                    long long b;
+                    u64 v;
+                    src.route(x[k], b, v);
+                    const bool valid = (u64)b < (u64)bins;
+                    bad |= !valid;
+                    r[k] = valid ? (int)(b >> kPartShift) : -1;
+                }
+            }
+        }
+        // per-thread counts, two 16-bit fields per word (ranges 2w and 2w + 1)
+        unsigned C[NW];
+        if constexpr (NW == 2) {
+            // up to four ranges: count in one word of 8-bit fields, then widen
+            unsigned c8 = 0u;
+#pragma unroll
+            for (int k = 0; k < kPartEPT; ++k)
+                if (r[k] >= 0) c8 += 1u << (r[k] << 3);
+            C[0] = (c8 & 0xffu) | ((c8 & 0xff00u) << 8);
+            C[1] = ((c8 >> 16) & 0xffu) | ((c8 >> 8) & 0xff0000u);
+        } else {
+#pragma unroll
+            for (int w = 0; w < NW; ++w) C[w] = 0u;
+#pragma unroll
+            for (int k = 0; k < kPartEPT; ++k) {
+                if (r[k] >= 0) {
+                    const unsigned one = 1u << ((r[k] & 1) << 4);
+                    // masked adds: no per-element indexing into C (which would
+                    // move it to local memory)
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) C[w] += one & (0u - (unsigned)((r[k] >> 1) == w));
+                }
+            }
+        }
+        // block-wide exclusive scan of the packed counts (fields never carry:
+        // a range holds at most kPartTile < 2^16 elements of a tile)
+        unsigned E[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            unsigned inc = C[w];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            E[w] = inc - C[w];
+            if (lane == 31) wtot[w][warp] = inc;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            // warp totals -> exclusive warp offsets per word; lane q < P picks
+            // up the tile's count of range q, then the range starts are scanned
+            unsigned tq = 0u;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+                const unsigned t0 = lane < kPartWarps ? wtot[w][lane] : 0u;
+                unsigned inc = t0;
+#pragma unroll
+                for (int o = 1; o < kPartWarps; o <<= 1) {
+                    const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                const unsigned tot = __shfl_sync(0xffffffffu, inc, kPartWarps - 1);
+                if (lane < kPartWarps) wtot[w][lane] = inc - t0;
+                if ((lane >> 1) == w) tq = (tot >> ((lane & 1) << 4)) & 0xffffu;
+            }
+            if (lane >= P) tq = 0u;
+            unsigned inc = tq;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            if (lane < P) {
+                rstart[lane] = inc - tq;
+                if (tq) atomicAdd(&counts[lane], tq);
+            }
+            if (lane == P - 1) rstart[P] = inc;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int w = 0; w < NW; ++w) E[w] += wtot[w][warp];
+        if constexpr (NW == 2) {
+            // this thread's first slot in each range, then a running byte count
+            const unsigned b0 = rstart[0] + (E[0] & 0xffffu), b1 = rstart[1] + (E[0] >> 16);
+            const unsigned b2 = rstart[2] + (E[1] & 0xffffu), b3 = rstart[3] + (E[1] >> 16);
+            unsigned run8 = 0u;
+#pragma unroll
+            for (int k = 0; k < kPartEPT; ++k) {
+                if (r[k] >= 0) {
+                    const int s8 = r[k] << 3;
+                    const unsigned local = (run8 >> s8) & 0xffu;
+                    run8 += 1u << s8;
+                    const unsigned b = (r[k] & 2) ? ((r[k] & 1) ? b3 : b2) : ((r[k] & 1) ? b1 : b0);
+                    in[b + local] = x[k];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kPartEPT; ++k) {
+                if (r[k] >= 0) {
+                    const int sh = (r[k] & 1) << 4;
+                    unsigned e = 0u;
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        const unsigned sel = 0u - (unsigned)((r[k] >> 1) == w);
+                        e |= E[w] & sel;
+                        E[w] += (1u << sh) & sel;
+                    }
+                    in[rstart[r[k]] + ((e >> sh) & 0xffffu)] = x[k];
+                }
+            }
+        }
+        // generic-proxy writes, then the bulk store reads the buffer
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int total = (int)rstart[P];
+            const unsigned sbytes = (unsigned)(total * 8) & ~15u;
+            if (sbytes) {
+                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(staged + e0),
+                             "r"(in0 + buf * kPartTile * 8), "r"(sbytes)
+                             : "memory");
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            }
+            if (total & 1) staged[e0 + total - 1] = in[total - 1];
+        }
+        if (threadIdx.x <= P) bounds[tile * (P + 1) + threadIdx.x] = (unsigned short)rstart[threadIdx.x];
+    }
+    if (timed_out && threadIdx.x == 0) {
+        // let the loads in flight land before the shared memory is released
+        for (int q = 0; q < kPartBufs; ++q)
+            if (tile + (int64_t)q * gridDim.x < ntiles)
+                mbar_wait_bounded(bar0 + 8 * ((it + q) % kPartBufs), ((it + q) / kPartBufs) & 1u);
+        raise_error(err, ERRBIT_TIMEOUT);
+    }
+    if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    if (bad) raise_error(err, ERRBIT_BOUNDS);
+}
+
+// Pass 2.  Each CTA takes one range -- ranges get CTAs in proportion to their
+// element counts, at least one each when non-empty -- and an equal share of
+// the tiles; the run bounds of up to kApplyChunk tiles at a time are staged in
+// shared memory, and warp w reads the runs of tiles w, w + 32, ... with
+// kApplyUnroll loads in flight per lane.  The limbs are flushed once, at the end.
+constexpr int kApplyChunk = 1024;
+
+template <class Src>
+__global__ void __launch_bounds__(kApplyThreads, 1)
+    hist_part_apply_kernel(Src src, const long long bins, const int P, const int64_t ntiles,
+                           const u64* __restrict__ staged, const unsigned short* __restrict__ bounds,
+                           unsigned* __restrict__ queue, u64* __restrict__ hist) {
+    extern __shared__ __align__(16) unsigned part_limbs[];
+    constexpr int per = 1 << kPartShift;
+    unsigned* lo = part_limbs;
+    unsigned* hi = part_limbs + per;
+    __shared__ int s_range, s_index, s_share;
+    __shared__ unsigned s_run[kApplyChunk];  // start | end << 16
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < 2 * per; i += kApplyThreads) part_limbs[i] = 0u;
+    if (threadIdx.x == 0) {
+        const volatile unsigned* cnt = queue + 32;
+        long long total = 0;
+        int nonempty = 0;
+        for (int r = 0; r < P; ++r) {
+            total += cnt[r];
+            nonempty += cnt[r] != 0u;
+        }
+        int range = -1, index = 0, share = 0;
+        if (total > 0) {
+            const long long spare = (long long)gridDim.x - nonempty;
+            long long cum = 0, first = 0;
+            for (int r = 0; r < P; ++r) {
+                const long long c = cnt[r];
+                if (c == 0) continue;
+                const long long a = 1 + spare * (cum + c) / total - spare * cum / total;
+                if ((long long)blockIdx.x >= first && (long long)blockIdx.x < first + a) {
+                    range = r;
+                    index = (int)(blockIdx.x - first);
+                    share = (int)a;
+                    break;
+                }
+                first += a;
+                cum += c;
+            }
+        }
+        s_range = range;
+        s_index = index;
+        s_share = share;
+    }
+    __syncthreads();
+    const int range = s_range;
+    if (range >= 0) {
+        const int64_t t_lo = ntiles * s_index / s_share, t_hi = ntiles * (s_index + 1) / s_share;
+        for (int64_t c0 = t_lo; c0 < t_hi; c0 += kApplyChunk) {
+            const int nb = (int)(t_hi - c0 < kApplyChunk ? t_hi - c0 : kApplyChunk);
+            for (int q = threadIdx.x; q < nb; q += kApplyThreads) {
+                const unsigned short* bt = bounds + (c0 + q) * (P + 1) + range;
+                s_run[q] = (unsigned)bt[0] | ((unsigned)bt[1] << 16);
+            }
+            __syncthreads();
+            for (int q = warp; q < nb; q += kApplyThreads / 32) {
+                const unsigned se = s_run[q];
+                const int s0 = (int)(se & 0xffffu), e = (int)(se >> 16);
+                const u64* run = staged + (c0 + q) * kPartTile;
+                auto apply1 = [&](u64 xv) {
+                    long long b;
+                    u64 v;
+                    src.route(xv, b, v);
+                    limb_add(lo, hi, (unsigned)(b & (per - 1)), v);
+                };
+                // odd ends one at a time; the pairs in between with 16-byte loads
+                const int a0 = (s0 + 1) & ~1, a1 = e & ~1;
+                if (lane == 0 && (s0 & 1) && s0 < e) apply1(run[s0]);
+                if (lane == 1 && (e & 1) && e - 1 >= a0) apply1(run[e - 1]);
+                const ulonglong2* pr = reinterpret_cast<const ulonglong2*>(run);
+                // 16-byte loads in flight per lane (fewer for the division route,
+                // which needs more registers)
+                constexpr int kU = Src::kMaskRoute ? kApplyUnroll : kApplyUnroll / 2;
+                for (int i = (a0 >> 1) + lane; i < (a1 >> 1); i += 32 * kU) {
+                    ulonglong2 x[kU];
+#pragma unroll
+                    for (int u = 0; u < kU; ++u)
+                        x[u] = i + 32 * u < (a1 >> 1) ? pr[i + 32 * u] : make_ulonglong2(0ULL, 0ULL);
+#pragma unroll
+                    for (int u = 0; u < kU; ++u) {
+                        if (i + 32 * u < (a1 >> 1)) {
+                            apply1(x[u].x);
+                            apply1(x[u].y);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        const long long first = (long long)range << kPartShift;
+        for (int i = threadIdx.x; i < per; i += kApplyThreads) {
+            const u64 sum = limb_value(lo, hi, i);
+            if (sum && first + i < bins) atomicAdd(&hist[first + i], sum);
+        }
+    }
+    // the last CTA to finish zeroes the counts for the next round
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(queue, 1u) == gridDim.x - 1) {
+            for (int r = 0; r < P; ++r) queue[32 + r] = 0u;
+            queue[0] = 0u;
+            __threadfence();
+        }
+    }
+}
+
 // ---- global atomics -----------------------------------------------------------
 template <class Src>
 __global__ void __launch_bounds__(kHistThreads, 2)
@@ -493,7 +876,7 @@ static int plan_cluster(const Device* d, long long bins, int G, HistPlan* p) {
     return HYD_CUDA_ERR_UNSUPPORTED;
 }
 
-static int plan_hist(const Device* d, long long bins, int strategy, bool packable, HistPlan* p) {
+static int plan_hist(const Device* d, long long bins, int64_t n, int strategy, bool packable, HistPlan* p) {
     const size_t bytes = (size_t)bins * 8;  // two 32-bit limbs per bin
     const size_t half = smem_half(d);
     const size_t optin = (size_t)d->max_smem_optin - 1024;
@@ -505,8 +888,8 @@ static int plan_hist(const Device* d, long long bins, int strategy, bool packabl
     p->smem = 0;
     if (strategy == HYD_SCATTER_AUTO) {
         const int tuned = tune_lookup_hist(bins);
-        if (tuned >= HYD_SCATTER_SMEM_WARP && tuned <= HYD_SCATTER_GLOBAL &&
-            (tuned != HYD_SCATTER_CLUSTER || packable))
+        if (tuned >= HYD_SCATTER_SMEM_WARP && tuned <= HYD_SCATTER_PARTITION &&
+            ((tuned != HYD_SCATTER_CLUSTER && tuned != HYD_SCATTER_PARTITION) || packable))
             strategy = tuned;
     }
     if (strategy == HYD_SCATTER_AUTO) {
@@ -514,9 +897,13 @@ static int plan_hist(const Device* d, long long bins, int strategy, bool packabl
             strategy = HYD_SCATTER_SMEM_WARP;
         } else if (bytes <= optin) {
             strategy = HYD_SCATTER_SMEM_BLOCK;
+        } else if (packable && bins <= (4LL << kPartShift) && n >= kPartAutoMin) {
+            // Measured on GB300 (B=65536, 2^27 elements): partition 0.58 ms,
+            // L2 atomics 0.84 ms, cluster pull 2.5 ms (per-lane DSMEM loads run
+            // at ~0.17/clk/SM).  Beyond four ranges, or on small inputs, the L2
+            // atomics win.
+            strategy = HYD_SCATTER_PARTITION;
         } else {
-            // Measured on GB300 (B=65536, 2^27 elements): L2 atomics 0.84 ms,
-            // cluster pull 2.5 ms (per-lane DSMEM loads run at ~0.17/clk/SM).
             strategy = HYD_SCATTER_GLOBAL;
         }
     }
@@ -559,6 +946,19 @@ static int plan_hist(const Device* d, long long bins, int strategy, bool packabl
                 if (plan_cluster(d, bins, G, p) == HYD_CUDA_OK) return HYD_CUDA_OK;
             }
             return set_error(HYD_CUDA_ERR_UNSUPPORTED, "CLUSTER: %lld bins exceed 16 CTAs of shared memory", bins);
+        }
+        case HYD_SCATTER_PARTITION: {
+            if (!packable)
+                return set_error(HYD_CUDA_ERR_UNSUPPORTED, "PARTITION: source is not single-word");
+            const long long P = (bins + (1LL << kPartShift) - 1) >> kPartShift;
+            if (P > kPartMaxRanges)
+                return set_error(HYD_CUDA_ERR_UNSUPPORTED, "PARTITION: %lld bins exceed %d ranges", bins,
+                                 kPartMaxRanges);
+            p->cluster = (int)P;
+            p->smem = (size_t)8 << kPartShift;
+            if (p->smem > optin) return set_error(HYD_CUDA_ERR_UNSUPPORTED, "PARTITION: shared memory too small");
+            p->blocks = d->sm_count;
+            return HYD_CUDA_OK;
         }
         case HYD_SCATTER_GLOBAL:
             p->blocks = d->sm_count * 2;
@@ -619,12 +1019,52 @@ static int launch_cluster(const Src& src, int64_t n, bool vec, long long bins, c
 }
 
 template <class Src>
+static int launch_partition(const Src& src, int64_t n, long long bins, const HistPlan& p, u64* hist, Device* d,
+                            cudaStream_t stream) {
+    if constexpr (Src::kPackable) {
+        const int P = p.cluster;
+        const int64_t seg = n < kPartMaxStage ? n : kPartMaxStage;
+        const int64_t max_tiles = (seg + kPartTile - 1) / kPartTile;
+        const size_t stage_bytes = (size_t)max_tiles * kPartTile * 8;
+        const size_t bounds_bytes = (size_t)max_tiles * (P + 1) * sizeof(unsigned short);
+        unsigned* counters = nullptr;
+        void* scratch = nullptr;
+        HYD_TRY(workspace(stream, stage_bytes + bounds_bytes, &counters, &scratch));
+        u64* staged = static_cast<u64*>(scratch);
+        unsigned short* bounds = reinterpret_cast<unsigned short*>(static_cast<unsigned char*>(scratch) + stage_bytes);
+        unsigned* queue = counters + kPartQueueWord;
+        auto stage_k = P <= 4 ? hist_part_stage_kernel<Src, 2>
+                       : P <= 8 ? hist_part_stage_kernel<Src, 4>
+                       : P <= 16 ? hist_part_stage_kernel<Src, 8> : hist_part_stage_kernel<Src, 16>;
+        auto apply_k = hist_part_apply_kernel<Src>;
+        HYD_TRY(allow_max_smem(stage_k, d));
+        HYD_TRY(allow_max_smem(apply_k, d));
+        // bulk copies need 16-byte aligned tiles (every tile start is, if the data is)
+        const bool bulk = (reinterpret_cast<uintptr_t>(src.data) & 15) == 0;
+        for (int64_t off = 0; off < n; off += kPartMaxStage) {
+            const int64_t m = n - off < kPartMaxStage ? n - off : kPartMaxStage;
+            const int64_t ntiles = (m + kPartTile - 1) / kPartTile;
+            Src part = src;
+            part.data += off;
+            const unsigned g1 = (unsigned)(ntiles < 2LL * d->sm_count ? ntiles : 2LL * d->sm_count);
+            stage_k<<<g1, kPartThreads, kPartStageSmem, stream>>>(part, m, bulk, bins, P, ntiles, staged,
+                                                                 bounds, queue + 32, d->d_err);
+            HYD_TRY(launch_check("weighted_histogram partition stage"));
+            apply_k<<<p.blocks, kApplyThreads, p.smem, stream>>>(part, bins, P, ntiles, staged, bounds, queue, hist);
+            HYD_TRY(launch_check("weighted_histogram partition apply"));
+        }
+        return HYD_CUDA_OK;
+    }
+    return set_error(HYD_CUDA_ERR_UNSUPPORTED, "PARTITION: source is not single-word");
+}
+
+template <class Src>
 static int hist_launch(const Src& src, int64_t n, bool vec, long long bins, u64* hist, int strategy,
                        cudaStream_t stream, const char* what) {
     Device* d = nullptr;
     HYD_TRY(device(&d));
     HistPlan p;
-    HYD_TRY(plan_hist(d, bins, strategy, Src::kPackable, &p));
+    HYD_TRY(plan_hist(d, bins, n, strategy, Src::kPackable, &p));
     const int64_t groups = (n + 3) / 4;
     const int64_t want = (groups + kHistThreads - 1) / kHistThreads;
     switch (p.strategy) {
@@ -638,6 +1078,9 @@ static int hist_launch(const Src& src, int64_t n, bool vec, long long bins, u64*
         }
         case HYD_SCATTER_CLUSTER:
             HYD_TRY(launch_cluster(src, n, vec, bins, p, hist, d, stream));
+            break;
+        case HYD_SCATTER_PARTITION:
+            HYD_TRY(launch_partition(src, n, bins, p, hist, d, stream));
             break;
         case HYD_SCATTER_GLOBAL:
             if (want < p.blocks) p.blocks = want < 1 ? 1 : (int)want;
@@ -670,7 +1113,7 @@ extern "C" int hyd_cuda_weighted_histogram_i64(const int64_t* data, int64_t n, i
     HYD_CHECK_ARG(bins > 0, "weighted_histogram: bins must be positive (got %lld)", (long long)bins);
     HYD_CHECK_ARG(hist != nullptr, "weighted_histogram: null histogram");
     HYD_CHECK_ARG(n == 0 || data != nullptr, "weighted_histogram: null data");
-    HYD_CHECK_ARG(strategy >= HYD_SCATTER_AUTO && strategy <= HYD_SCATTER_GLOBAL,
+    HYD_CHECK_ARG(strategy >= HYD_SCATTER_AUTO && strategy <= HYD_SCATTER_PARTITION,
                   "weighted_histogram: unknown strategy %d", strategy);
     HYD_CHECK_ARG(bins <= (1LL << 31), "weighted_histogram: bins beyond 2^31 unsupported");
     if (n == 0) return HYD_CUDA_OK;
@@ -687,13 +1130,29 @@ extern "C" int hyd_cuda_weighted_histogram_i64(const int64_t* data, int64_t n, i
                        "weighted_histogram_i64");
 }
 
+extern "C" int hyd_cuda_weighted_histogram_plan(int64_t n, int64_t bins, int strategy, int* chosen, int* launches) {
+    HYD_CHECK_ARG(n >= 0 && bins > 0 && bins <= (1LL << 31), "weighted_histogram_plan: bad shape");
+    HYD_CHECK_ARG(strategy >= HYD_SCATTER_AUTO && strategy <= HYD_SCATTER_PARTITION,
+                  "weighted_histogram_plan: unknown strategy %d", strategy);
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    HistPlan p;
+    HYD_TRY(plan_hist(d, bins, n, strategy, true, &p));
+    if (chosen) *chosen = p.strategy;
+    if (launches) {
+        const int64_t rounds = (n + kPartMaxStage - 1) / kPartMaxStage;
+        *launches = n == 0 ? 0 : (p.strategy == HYD_SCATTER_PARTITION ? (int)(2 * rounds) : 1);
+    }
+    return HYD_CUDA_OK;
+}
+
 extern "C" int hyd_cuda_scatter_add_i64(const int64_t* idx, const int64_t* vals, int64_t n,
                                         int64_t* dst, int64_t dst_n, int strategy, void* stream) {
     HYD_CHECK_ARG(n >= 0, "scatter_add_i64: negative length");
     HYD_CHECK_ARG(dst_n > 0, "scatter_add_i64: empty destination");
     HYD_CHECK_ARG(dst != nullptr, "scatter_add_i64: null destination");
     HYD_CHECK_ARG(n == 0 || (idx != nullptr && vals != nullptr), "scatter_add_i64: null input");
-    HYD_CHECK_ARG(strategy >= HYD_SCATTER_AUTO && strategy <= HYD_SCATTER_GLOBAL,
+    HYD_CHECK_ARG(strategy >= HYD_SCATTER_AUTO && strategy <= HYD_SCATTER_PARTITION,
                   "scatter_add_i64: unknown strategy %d", strategy);
     HYD_CHECK_ARG(dst_n <= (1LL << 31), "scatter_add_i64: destination beyond 2^31 unsupported");
     if (n == 0) return HYD_CUDA_OK;

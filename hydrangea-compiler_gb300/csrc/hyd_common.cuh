@@ -168,4 +168,42 @@ struct DivMod64 {
     }
 };
 
+// ---- mbarrier + bulk asynchronous copies (shared by the TMA kernels) ----------
+constexpr unsigned kTmaWaitLimit = 1u << 22;  // polls before a wait gives up
+
+__device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned addr, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test_wait(unsigned addr, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait (non-blocking polls with a short sleep between them, about a
+// quarter of a second in total); false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity) {
+    for (unsigned it = 0; it < kTmaWaitLimit; ++it) {
+        if (mbar_test_wait(addr, parity)) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+// One-dimensional bulk copy global -> shared, completing on an mbarrier.  Both
+// addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_load_1d(unsigned dst, const void* src, unsigned bytes, unsigned mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(mbar)
+        : "memory");
+}
+
 }  // namespace hyd

@@ -77,7 +77,6 @@ __global__ void __launch_bounds__(256) stencil_plain_kernel(const double* __rest
 // input box adds a 1-row halo above/below and a 2-column halo left/right (the
 // TMA x coordinate must stay 16-byte aligned).
 constexpr int kStThreads = 256;
-constexpr unsigned kTmaWaitLimit = 1u << 22;  // polls before a wait gives up
 
 template <int TH, int TW>
 struct TileShape {
@@ -92,32 +91,6 @@ struct TileShape {
     static_assert(kBoxW <= 256 && kBoxH <= 256, "TMA box limit");
 };
 
-__device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned addr, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_test_wait(unsigned addr, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait (non-blocking polls with a short sleep between them, about a
-// quarter of a second in total); false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity) {
-    for (unsigned it = 0; it < kTmaWaitLimit; ++it) {
-        if (mbar_test_wait(addr, parity)) return true;
-        __nanosleep(64);
-    }
-    return false;
-}
 __device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap* map, int x, int y,
                                             unsigned mbar) {
     asm volatile(

@@ -19,7 +19,7 @@ ERR_INVALID, ERR_NOMEM, ERR_CUDA, ERR_NO_DEVICE, ERR_BOUNDS = 1, 2, 3, 4, 5
 ERR_TIMEOUT, ERR_BUDGET, ERR_CANCELLED, ERR_UNSUPPORTED = 6, 7, 8, 9
 
 STENCIL_LAPLACIAN, STENCIL_JACOBI, STENCIL_HEAT, STENCIL_HEAT_EXAMPLE = 0, 1, 2, 3
-SCATTER_AUTO, SCATTER_SMEM_WARP, SCATTER_SMEM_BLOCK, SCATTER_CLUSTER, SCATTER_GLOBAL = 0, 1, 2, 3, 4
+SCATTER_AUTO, SCATTER_SMEM_WARP, SCATTER_SMEM_BLOCK, SCATTER_CLUSTER, SCATTER_GLOBAL, SCATTER_PARTITION = 0, 1, 2, 3, 4, 5
 
 _p = C.c_void_p
 _i64 = C.c_int64
@@ -43,6 +43,7 @@ SIGNATURES = {
     "hyd_cuda_sum_f64": (_i, [_p, _i64, _p, _p]),
     "hyd_cuda_dot_f64_noalloc": (_i, [_p, _p, _i64, _p, _p]),
     "hyd_cuda_weighted_histogram_i64": (_i, [_p, _i64, _i64, _p, _i, _p]),
+    "hyd_cuda_weighted_histogram_plan": (_i, [_i64, _i64, _i, _p, _p]),
     "hyd_cuda_scatter_add_i64": (_i, [_p, _p, _i64, _p, _i64, _i, _p]),
     "hyd_cuda_scatter_add_f64": (_i, [_p, _p, _i64, _p, _i64, _p]),
     "hyd_cuda_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _p]),
@@ -216,6 +217,16 @@ def weighted_histogram(data, hist, strategy=SCATTER_AUTO, stream=None):
          strategy, stream_handle(stream))
 
 
+def weighted_histogram_plan(n, bins, strategy=SCATTER_AUTO):
+    """(strategy a call of this shape runs, kernels it launches)."""
+    chosen, launches = C.c_int(0), C.c_int(0)
+    call("hyd_cuda_weighted_histogram_plan", n, bins, strategy, C.byref(chosen), C.byref(launches))
+    return chosen.value, launches.value
+
+
+STRATEGY_NAMES = {0: "AUTO", 1: "SMEM_WARP", 2: "SMEM_BLOCK", 3: "CLUSTER", 4: "GLOBAL", 5: "PARTITION"}
+
+
 def scatter_add_i64(idx, vals, dst, strategy=SCATTER_AUTO, stream=None):
     call("hyd_cuda_scatter_add_i64", ptr(idx), ptr(vals), idx.numel(), ptr(dst), dst.numel(),
          strategy, stream_handle(stream))
@@ -254,7 +265,7 @@ def autotune_stencil2d(kind, h, w, reps=5):
 def autotune_histogram(n, bins, reps=5):
     import numpy as np
     best = C.c_int(-1)
-    times = np.zeros(5)
+    times = np.zeros(6)
     call("hyd_cuda_autotune_histogram", n, bins, reps, C.byref(best), times.ctypes.data)
     return best.value, times
 

@@ -120,10 +120,16 @@ typedef enum {
     HYD_SCATTER_SMEM_WARP = 1,     /* per-warp shared-memory bins */
     HYD_SCATTER_SMEM_BLOCK = 2,    /* one shared-memory copy per block */
     HYD_SCATTER_CLUSTER = 3,       /* bins spread over a thread-block cluster's DSMEM */
-    HYD_SCATTER_GLOBAL = 4         /* global atomics (bins beyond on-chip memory) */
+    HYD_SCATTER_GLOBAL = 4,        /* global atomics (bins beyond on-chip memory) */
+    HYD_SCATTER_PARTITION = 5      /* staging pass grouping elements by bin range, then one
+                                      shared-memory pass per range (single-word sources) */
 } hyd_scatter_strategy_t;
 int hyd_cuda_weighted_histogram_i64(const int64_t* data, int64_t n, int64_t bins,
                                     int64_t* hist, int strategy, void* stream);
+/* The strategy a weighted_histogram call of this shape runs (AUTO resolved,
+ * tuned choices included) and how many kernels it launches.  No counterpart
+ * in the reference; for reporting and tests. */
+int hyd_cuda_weighted_histogram_plan(int64_t n, int64_t bins, int strategy, int* chosen, int* launches);
 /* Unfused scatter (+) over materialised routes and values (Lowering.hs:
  * 1408-1430): dst[idx[i]] += vals[i].  int64 variant is order-independent
  * (bit-exact); the float variant accumulates with fp64 atomics and is
@@ -181,7 +187,7 @@ int hyd_cuda_tune_set_cache_path(const char* path);     /* reloads the table fro
 int hyd_cuda_tune_record(const char* device, const char* kernel, const char* klass, int choice, double us);
 int hyd_cuda_tune_query(const char* device, const char* kernel, const char* klass);  /* -1 if absent */
 /* Time every stencil variant (times_us[7], may be NULL) / histogram strategy
- * (times_us[5], index = strategy, -1 when it cannot run) on scratch inputs and
+ * (times_us[6], index = strategy, -1 when it cannot run) on scratch inputs and
  * record the fastest in *best. */
 int hyd_cuda_autotune_stencil2d(int kind, int64_t h, int64_t w, int reps, int* best, double* times_us);
 int hyd_cuda_autotune_histogram(int64_t n, int64_t bins, int reps, int* best, double* times_us);

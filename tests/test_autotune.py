@@ -50,7 +50,7 @@ def test_autotune_stencil_records_choice(hc, dev):
 def test_autotune_histogram_records_choice(hc, orc, dev):
     import torch
     best, times = hc.autotune_histogram(1 << 20, 4096, reps=3)
-    assert best in (1, 2, 3, 4)
+    assert best in (1, 2, 3, 4, 5)
     assert hc.lib().hyd_cuda_tune_query(None, b"weighted_histogram", b"b12") == best
     # the AUTO path now uses the tuned strategy and stays bit-exact
     data = torch.empty(100_000, dtype=torch.int64, device=dev)

@@ -6,7 +6,8 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-STRATS = ["SCATTER_AUTO", "SCATTER_SMEM_WARP", "SCATTER_SMEM_BLOCK", "SCATTER_CLUSTER", "SCATTER_GLOBAL"]
+STRATS = ["SCATTER_AUTO", "SCATTER_SMEM_WARP", "SCATTER_SMEM_BLOCK", "SCATTER_CLUSTER", "SCATTER_GLOBAL",
+          "SCATTER_PARTITION"]
 
 
 def _data(hc, n, dev, seed=2, bound=1 << 20):
@@ -112,3 +113,52 @@ def test_unfused_scatter_add_f64(hc, orc, dev):
     ref = np.zeros(100)
     orc.lib().orc_scatter_add_f64(idx, vals, 5000, ref, 100)
     assert np.allclose(dst.cpu().numpy(), ref, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("bins", [16385, 65536, 65521, 262144, 1 << 19])
+@pytest.mark.parametrize("n", [1, 4095, 4097, 1_000_003])
+def test_partition_ragged_and_unaligned(hc, orc, dev, bins, n):
+    base = _data(hc, n + 1, dev, seed=11)
+    for data in (base[:n], base[1:]):  # 32-byte aligned and 8-byte aligned starts
+        assert np.array_equal(_run(hc, data, bins, hc.SCATTER_PARTITION, dev),
+                              orc.weighted_hist(data.cpu().numpy(), bins))
+
+
+def test_partition_skewed_ranges(hc, orc, dev):
+    # every element in one bin range, then two ranges of very different sizes
+    data = _data(hc, 3_000_000, dev, seed=5, bound=1 << 14)
+    assert np.array_equal(_run(hc, data, 65536, hc.SCATTER_PARTITION, dev),
+                          orc.weighted_hist(data.cpu().numpy(), 65536))
+    data2 = torch.cat([data, _data(hc, 1000, dev, seed=6) + (1 << 15)])
+    assert np.array_equal(_run(hc, data2, 65536, hc.SCATTER_PARTITION, dev),
+                          orc.weighted_hist(data2.cpu().numpy(), 65536))
+
+
+def test_partition_out_of_range_and_repeat(hc, orc, dev):
+    data = _data(hc, 100_000, dev, seed=8)
+    data[::1000] = -3  # negative x with a non-zero remainder: out of range
+    hist = torch.zeros(65536, dtype=torch.int64, device=dev)
+    hc.weighted_histogram(data, hist, strategy=hc.SCATTER_PARTITION)
+    assert hc.device_check() == hc.ERR_BOUNDS
+    keep = data.cpu().numpy()
+    keep = keep[keep >= 0]
+    assert np.array_equal(hist.cpu().numpy(), orc.weighted_hist(keep, 65536))
+    # the work queue resets itself: a second call adds the same again
+    hc.weighted_histogram(data, hist, strategy=hc.SCATTER_PARTITION)
+    hc.device_check()
+    assert np.array_equal(hist.cpu().numpy(), 2 * orc.weighted_hist(keep, 65536))
+
+
+def test_partition_more_than_one_staging_round(hc, orc, dev):
+    n = (1 << 27) + 5000  # beyond one staging round of 2^27 elements
+    data = _data(hc, n, dev, seed=3)
+    assert np.array_equal(_run(hc, data, 65536, hc.SCATTER_PARTITION, dev),
+                          orc.weighted_hist(data.cpu().numpy(), 65536))
+
+
+def test_plan_reports_strategy_and_launches(hc, dev):
+    assert hc.weighted_histogram_plan(1 << 27, 64) == (hc.SCATTER_SMEM_WARP, 1)
+    assert hc.weighted_histogram_plan(1 << 27, 65536) == (hc.SCATTER_PARTITION, 2)
+    assert hc.weighted_histogram_plan((1 << 28) + 1, 65536) == (hc.SCATTER_PARTITION, 6)
+    assert hc.weighted_histogram_plan(1 << 16, 65536) == (hc.SCATTER_GLOBAL, 1)
+    assert hc.weighted_histogram_plan(1 << 27, 1 << 20) == (hc.SCATTER_GLOBAL, 1)
