@@ -45,6 +45,8 @@ def parse_args():
     p.add_argument("--no-suite", action="store_true",
                    help="skip the other configurations (dot, heat_2d, batched, serving)")
     p.add_argument("--serve-requests", type=int, default=100_000)
+    p.add_argument("--no-e2e", action="store_true",
+                   help="skip the host-buffer (e2e) leg; for profiler runs of the device kernels only")
     return p.parse_args()
 
 
@@ -226,37 +228,41 @@ def run_gpu(args):
     achieved = bytes_per_launch[dom] / (avg[dom] / 1e3) / 1e9
     traffic = profile_traffic("weighted_histogram_i64_B%d" % dom)
 
-    # e2e through the C-ABI host-pointer entry point: H2D of the step's input from
-    # pinned host memory and D2H of the histogram inside the timed region.
-    pinned = torch.empty(N_ELEMS, dtype=torch.int64, pin_memory=True)
-    pinned.copy_(data)
-    out_host = {b: torch.zeros(b, dtype=torch.int64, pin_memory=True) for b in BINS}
-    e2e_steps = max(3, min(args.steps, 20))
+    def run_e2e():
+        # e2e through the C-ABI host-pointer entry point: H2D of the step's input from
+        # pinned host memory and D2H of the histogram inside the timed region.
+        pinned = torch.empty(N_ELEMS, dtype=torch.int64, pin_memory=True)
+        pinned.copy_(data)
+        out_host = {b: torch.zeros(b, dtype=torch.int64, pin_memory=True) for b in BINS}
+        e2e_steps = max(3, min(args.steps, 20))
 
-    def e2e_step():
+        def e2e_step():
+            for b in BINS:
+                hc.check(L.hyd_cuda_weighted_histogram_host(pinned.data_ptr(), N_ELEMS, b,
+                                                            out_host[b].data_ptr(), 0))
+        for _ in range(2):
+            e2e_step()
+        if dist:
+            dist.barrier()
+        te = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_s = time.perf_counter() - te
+        if dist:
+            t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
         for b in BINS:
-            hc.check(L.hyd_cuda_weighted_histogram_host(pinned.data_ptr(), N_ELEMS, b,
-                                                        out_host[b].data_ptr(), 0))
-    for _ in range(2):
-        e2e_step()
-    if dist:
-        dist.barrier()
-    te = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_s = time.perf_counter() - te
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    for b in BINS:
-        assert torch.equal(out_host[b], hists[b].cpu()), "e2e result differs"
-    e2e_value = world * bytes_per_step * e2e_steps / e2e_s / 1e9
+            assert torch.equal(out_host[b], hists[b].cpu()), "e2e result differs"
+        e2e_value = world * bytes_per_step * e2e_steps / e2e_s / 1e9
+        del pinned, out_host
+        return e2e_value, e2e_steps
+
+    e2e_value, e2e_steps = (None, 0) if args.no_e2e else run_e2e()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(host)
-    del pinned, out_host
     suite = None
     if rank == 0 and world == 1 and not args.no_suite:
         del data, hists
@@ -300,7 +306,7 @@ def run_gpu(args):
                 "traffic": traffic,
                 "algorithmic_bytes_per_launch": bytes_per_launch[dom],
             },
-            "e2e": {
+            "e2e": None if e2e_value is None else {
                 "value": round(e2e_value, 2), "unit": "GB/s",
                 "h2d_bytes_per_step": 8 * N_ELEMS * len(BINS),
                 "d2h_bytes_per_step": 8 * sum(BINS),

@@ -552,12 +552,14 @@ __global__ void __launch_bounds__(kPartThreads, 2)
                 }
             }
         }
+        // high words of the present elements: a tile whose high words are all
+        // zero is staged as 4-byte records
+        unsigned hi_or = 0u;
+#pragma unroll
+        for (int k = 0; k < kPartEPT; ++k) hi_or |= r[k] == 0 ? (unsigned)(x[k] >> 32) : 0u;
         bool fast = false;
         if constexpr (Src::kMaskRoute) {
             // all present elements non-negative: the bin is the masked low word
-            unsigned hi_or = 0u;
-#pragma unroll
-            for (int k = 0; k < kPartEPT; ++k) hi_or |= r[k] == 0 ? (unsigned)(x[k] >> 32) : 0u;
             if ((int)hi_or >= 0) {
                 fast = true;
                 const unsigned m = src.mask32();
@@ -617,7 +619,7 @@ __global__ void __launch_bounds__(kPartThreads, 2)
             E[w] = inc - C[w];
             if (lane == 31) wtot[w][warp] = inc;
         }
-        __syncthreads();
+        const bool wide = __syncthreads_or(hi_or != 0u);
         if (warp == 0) {
             // warp totals -> exclusive warp offsets per word; lane q < P picks
             // up the tile's count of range q, then the range starts are scanned
@@ -663,7 +665,8 @@ __global__ void __launch_bounds__(kPartThreads, 2)
                     const unsigned local = (run8 >> s8) & 0xffu;
                     run8 += 1u << s8;
                     const unsigned b = (r[k] & 2) ? ((r[k] & 1) ? b3 : b2) : ((r[k] & 1) ? b1 : b0);
-                    in[b + local] = x[k];
+                    if (wide) in[b + local] = x[k];
+                    else reinterpret_cast<unsigned*>(in)[b + local] = (unsigned)x[k];
                 }
             }
         } else {
@@ -678,7 +681,9 @@ __global__ void __launch_bounds__(kPartThreads, 2)
                         e |= E[w] & sel;
                         E[w] += (1u << sh) & sel;
                     }
-                    in[rstart[r[k]] + ((e >> sh) & 0xffffu)] = x[k];
+                    const unsigned slot = rstart[r[k]] + ((e >> sh) & 0xffffu);
+                    if (wide) in[slot] = x[k];
+                    else reinterpret_cast<unsigned*>(in)[slot] = (unsigned)x[k];
                 }
             }
         }
@@ -686,17 +691,24 @@ __global__ void __launch_bounds__(kPartThreads, 2)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
-            const int total = (int)rstart[P];
-            const unsigned sbytes = (unsigned)(total * 8) & ~15u;
+            const unsigned esz = wide ? 8u : 4u;
+            const unsigned all = rstart[P] * esz;
+            const unsigned sbytes = all & ~15u;
             if (sbytes) {
                 asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(staged + e0),
                              "r"(in0 + buf * kPartTile * 8), "r"(sbytes)
                              : "memory");
                 asm volatile("cp.async.bulk.commit_group;" ::: "memory");
             }
-            if (total & 1) staged[e0 + total - 1] = in[total - 1];
+            // the last partial 16 bytes
+            unsigned char* dst = reinterpret_cast<unsigned char*>(staged + e0);
+            const unsigned char* srcb = reinterpret_cast<const unsigned char*>(in);
+            for (unsigned b = sbytes; b < all; b += 4)
+                *reinterpret_cast<unsigned*>(dst + b) = *reinterpret_cast<const unsigned*>(srcb + b);
         }
-        if (threadIdx.x <= P) bounds[tile * (P + 1) + threadIdx.x] = (unsigned short)rstart[threadIdx.x];
+        // run bounds; bit 15 marks a tile staged as 4-byte records
+        if (threadIdx.x <= P)
+            bounds[tile * (P + 1) + threadIdx.x] = (unsigned short)(rstart[threadIdx.x] | (wide ? 0u : 0x8000u));
     }
     if (timed_out && threadIdx.x == 0) {
         // let the loads in flight land before the shared memory is released
@@ -767,12 +779,12 @@ __global__ void __launch_bounds__(kApplyThreads, 1)
             const int nb = (int)(t_hi - c0 < kApplyChunk ? t_hi - c0 : kApplyChunk);
             for (int q = threadIdx.x; q < nb; q += kApplyThreads) {
                 const unsigned short* bt = bounds + (c0 + q) * (P + 1) + range;
-                s_run[q] = (unsigned)bt[0] | ((unsigned)bt[1] << 16);
+                s_run[q] = (unsigned)bt[0] | ((unsigned)bt[1] << 16);  // bit 15 of each: 4-byte records
             }
             __syncthreads();
             for (int q = warp; q < nb; q += kApplyThreads / 32) {
                 const unsigned se = s_run[q];
-                const int s0 = (int)(se & 0xffffu), e = (int)(se >> 16);
+                const int s0 = (int)(se & 0x7fffu), e = (int)((se >> 16) & 0x7fffu);
                 const u64* run = staged + (c0 + q) * kPartTile;
                 auto apply1 = [&](u64 xv) {
                     long long b;
@@ -780,6 +792,35 @@ __global__ void __launch_bounds__(kApplyThreads, 1)
                     src.route(xv, b, v);
                     limb_add(lo, hi, (unsigned)(b & (per - 1)), v);
                 };
+                if (se & 0x8000u) {
+                    // 4-byte records: ragged ends one at a time, 16-byte loads between
+                    const unsigned* run32 = reinterpret_cast<const unsigned*>(run);
+                    const int a0 = (s0 + 3) & ~3, a1 = e & ~3;
+                    if (a0 >= a1) {
+                        if (lane < e - s0) apply1(run32[s0 + lane]);
+                        continue;
+                    }
+                    if (lane < a0 - s0) apply1(run32[s0 + lane]);
+                    if (lane < e - a1) apply1(run32[a1 + lane]);
+                    const uint4* p4 = reinterpret_cast<const uint4*>(run32);
+                    constexpr int kU4 = Src::kMaskRoute ? kApplyUnroll : kApplyUnroll / 4;
+                    for (int i = (a0 >> 2) + lane; i < (a1 >> 2); i += 32 * kU4) {
+                        uint4 y[kU4];
+#pragma unroll
+                        for (int u = 0; u < kU4; ++u)
+                            y[u] = i + 32 * u < (a1 >> 2) ? p4[i + 32 * u] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                        for (int u = 0; u < kU4; ++u) {
+                            if (i + 32 * u < (a1 >> 2)) {
+                                apply1(y[u].x);
+                                apply1(y[u].y);
+                                apply1(y[u].z);
+                                apply1(y[u].w);
+                            }
+                        }
+                    }
+                    continue;
+                }
                 // odd ends one at a time; the pairs in between with 16-byte loads
                 const int a0 = (s0 + 1) & ~1, a1 = e & ~1;
                 if (lane == 0 && (s0 & 1) && s0 < e) apply1(run[s0]);

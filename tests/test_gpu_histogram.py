@@ -162,3 +162,17 @@ def test_plan_reports_strategy_and_launches(hc, dev):
     assert hc.weighted_histogram_plan((1 << 28) + 1, 65536) == (hc.SCATTER_PARTITION, 6)
     assert hc.weighted_histogram_plan(1 << 16, 65536) == (hc.SCATTER_GLOBAL, 1)
     assert hc.weighted_histogram_plan(1 << 27, 1 << 20) == (hc.SCATTER_GLOBAL, 1)
+
+
+@pytest.mark.parametrize("bins", [65536, 40000])
+def test_partition_mixed_record_widths(hc, orc, dev, bins):
+    # tiles of small values are staged as 4-byte records, tiles holding a value
+    # with a non-zero high word as 8-byte records; both must sum alike
+    data = _data(hc, 50_000, dev, seed=12)
+    big = _data(hc, 50_000, dev, seed=13, bound=1 << 62)
+    data[4096:8192] = big[4096:8192]          # one whole wide tile
+    data[20_000] = big[20_000]                # one wide element in a narrow-looking tile
+    data[30_001:30_003] = (1 << 32) + 5       # high word exactly 1
+    for d in (data, data[3:]):
+        assert np.array_equal(_run(hc, d, bins, hc.SCATTER_PARTITION, dev),
+                              orc.weighted_hist(d.cpu().numpy(), bins))
