@@ -57,6 +57,21 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x, dist, device):
+    """The largest of every rank's x (the job's time is its slowest replica)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gbs(world, bytes_per_step, steps, elapsed_s):
+    """Aggregate GB/s of `world` replicas that each ran `steps` steps."""
+    return world * bytes_per_step * steps / elapsed_s / 1e9
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -206,10 +221,7 @@ def run_gpu(args):
     for k in range(args.steps):
         for i, b in enumerate(BINS):
             per_kernel[b].append(ev_pairs[k][i][0].elapsed_time(ev_pairs[k][i][1]))
-    if dist:
-        t = torch.tensor([elapsed_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, dev)
 
     # correctness guard on the measured buffers (bins sum = sum of squares)
     host = data.cpu().numpy()
@@ -221,7 +233,7 @@ def run_gpu(args):
     plans = {b: hc.weighted_histogram_plan(N_ELEMS, b) for b in BINS}
     bytes_per_launch = {b: 8 * N_ELEMS + 8 * b for b in BINS}
     bytes_per_step = sum(bytes_per_launch.values())
-    value = world * bytes_per_step * args.steps / (elapsed_ms / 1e3) / 1e9
+    value = whole_job_gbs(world, bytes_per_step, args.steps, elapsed_ms / 1e3)
     peak, peak_src = measured_peak()
     avg = {b: statistics.mean(per_kernel[b]) for b in BINS}
     dom = max(BINS, key=lambda b: avg[b])
@@ -248,13 +260,10 @@ def run_gpu(args):
         for _ in range(e2e_steps):
             e2e_step()
         e2e_s = time.perf_counter() - te
-        if dist:
-            t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dist, dev)
         for b in BINS:
             assert torch.equal(out_host[b], hists[b].cpu()), "e2e result differs"
-        e2e_value = world * bytes_per_step * e2e_steps / e2e_s / 1e9
+        e2e_value = whole_job_gbs(world, bytes_per_step, e2e_steps, e2e_s)
         del pinned, out_host
         return e2e_value, e2e_steps
 

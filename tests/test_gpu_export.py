@@ -1,0 +1,83 @@
+"""GPU parity of the embedding boundary: host-pointer entry points (the
+host->device copies pipelined against the kernels in chunks), the
+`hyd_export_<name>` symbols on the reference's `hyd_array_t`
+(CodegenC.hs:372-460) and arrays that the reference's `hyd_array_free`
+(runtime/hydrangea_runtime.h:333-343) releases."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LIBC = C.CDLL(None)
+LIBC.free.argtypes = [C.c_void_p]
+
+
+def _array_free(hc, p):
+    """What the reference runtime's hyd_array_free does: drop one reference
+    to the storage, free data + storage at zero, then the header."""
+    a = p.contents
+    st = a.storage.contents
+    st.refcount -= 1
+    if st.refcount == 0:
+        LIBC.free(st.data)
+        LIBC.free(C.cast(a.storage, C.c_void_p))
+    LIBC.free(C.cast(p, C.c_void_p))
+
+
+@pytest.mark.parametrize("n", [0, 5, 4099, 20_000_003])  # the last spans three 64 MiB chunks
+@pytest.mark.parametrize("bins", [64, 65536])
+def test_histogram_host_path(hc, orc, n, bins):
+    data = orc.uniform_i64(n, 21, 1 << 20) if n else np.zeros(0, np.int64)
+    got = hc.weighted_histogram_host(data, bins)
+    ref = orc.weighted_hist(data, bins) if n else np.zeros(bins, np.int64)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("n", [0, 1, 1000, 20_000_001])
+def test_dot_host_path(hc, orc, n):
+    rng = np.random.default_rng(22)
+    xs, ys = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    got = hc.dot_f64_host(xs, ys)
+    ref = orc.dot_compensated(xs, ys) if n else 0.0
+    assert abs(got - ref) <= 1e-12 * max(1.0, np.abs(xs * ys).sum())
+
+
+def test_export_symbols_on_hyd_array(hc, orc):
+    L = hc.lib()
+    data = orc.uniform_i64(100_000, 23, 1 << 20)
+    fn = L.hyd_export_weighted_histogram
+    fn.restype = C.POINTER(hc.Array)
+    fn.argtypes = [C.POINTER(hc.Array), C.c_int64]
+    arr = hc.make_array(data)
+    out = fn(C.byref(arr), 4096)
+    a = out.contents
+    assert a.shape.ndims == 1 and a.shape.elems[0] == 4096 and a.elem_size == 8
+    assert a.storage.contents.refcount == 1
+    got = np.ctypeslib.as_array(C.cast(a.data, C.POINTER(C.c_int64)), shape=(4096,)).copy()
+    assert np.array_equal(got, orc.weighted_hist(data, 4096))
+    _array_free(hc, out)  # allocated with malloc/calloc, as the reference allocator
+
+    xs, ys = np.linspace(-1, 1, 7777), np.linspace(2, -2, 7777)
+    dot = L.hyd_export_dot
+    dot.restype = C.c_double
+    dot.argtypes = [C.POINTER(hc.Array), C.POINTER(hc.Array)]
+    ax, ay = hc.make_array(xs), hc.make_array(ys)
+    assert abs(dot(C.byref(ax), C.byref(ay)) - orc.dot_compensated(xs, ys)) < 1e-12 * 7777
+
+
+def test_runtime_array_alloc_is_zeroed_and_freeable(hc):
+    L = hc.lib()
+    f = L.hyd_cuda_array_alloc
+    f.restype = C.POINTER(hc.Array)
+    f.argtypes = [hc.Tuple, C.c_size_t]
+    t = hc.Tuple()
+    t.ndims = 2
+    t.elems[0], t.elems[1] = 3, 5
+    p = f(t, 8)
+    a = p.contents
+    assert a.shape.ndims == 2 and a.elem_size == 8
+    vals = np.ctypeslib.as_array(C.cast(a.data, C.POINTER(C.c_int64)), shape=(15,))
+    assert not vals.any()
+    _array_free(hc, p)
