@@ -463,6 +463,7 @@ constexpr int kPartMaxRanges = 32;
 constexpr int kPartShift = 14;  // 16384 bins (128 KB of limbs) per range
 // three tile buffers (bulk-loaded, grouped in place, bulk-stored) + mbarriers
 constexpr int kPartBufs = 3;
+constexpr int kPartCtasPerSm = 2;
 constexpr size_t kPartStageSmem = kPartBufs * (size_t)kPartTile * 8 + 8 * kPartBufs;
 constexpr int kApplyThreads = 1024;
 constexpr int kApplyUnroll = 8;
@@ -481,7 +482,7 @@ constexpr int kPartQueueWord = 64;
 // thread its offset inside every range; the elements, held in registers, are
 // then written back into the buffer they were read from in range order.
 template <class Src, int NW>
-__global__ void __launch_bounds__(kPartThreads, 2)
+__global__ void __launch_bounds__(kPartThreads, kPartCtasPerSm)
     hist_part_stage_kernel(Src src, const int64_t n, const bool bulk, const long long bins, const int P,
                            const int64_t ntiles, u64* __restrict__ staged, unsigned short* __restrict__ bounds,
                            unsigned* __restrict__ counts, unsigned* err) {
@@ -491,6 +492,7 @@ __global__ void __launch_bounds__(kPartThreads, 2)
     const unsigned bar0 = in0 + kPartBufs * kPartTile * 8;
     __shared__ unsigned wtot[NW][kPartWarps];
     __shared__ unsigned rstart[kPartMaxRanges + 1];
+    __shared__ unsigned scur[NW == 2 ? 4 * kPartThreads : 1];  // per-thread range cursors
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     bool bad = false;
     if (threadIdx.x == 0) {
@@ -523,7 +525,9 @@ __global__ void __launch_bounds__(kPartThreads, 2)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(ahead, (int)((it + kPartBufs - 1) % kPartBufs));
         }
-        const bool arrived = mbar_wait_bounded(bar0 + 8 * buf, (it / kPartBufs) & 1u);
+        // one thread polls (acquire on the mbarrier phase); the block barrier
+        // then orders the landed tile before every thread's reads
+        const bool arrived = threadIdx.x == 0 ? mbar_wait_bounded(bar0 + 8 * buf, (it / kPartBufs) & 1u) : true;
         if (__syncthreads_or(!arrived)) {
             timed_out = true;
             break;
@@ -534,16 +538,36 @@ __global__ void __launch_bounds__(kPartThreads, 2)
         u64* const in = inbuf + buf * kPartTile;
         u64 x[kPartEPT];
         int r[kPartEPT];  // range; -1: no element or out of range
+        // a full tile in shared memory whose elements all route by the mask
+        // ("clean") needs no per-element presence or range checks
+        const bool full = have == kPartTile;
+        unsigned hi_or = 0u;  // high words: all zero -> staged as 4-byte records
+        bool fast = false;
+        if (full) {
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int j0 = 4 * (threadIdx.x + h * kPartThreads);
-            if (j0 + 4 <= have) {
+            for (int h = 0; h < 2; ++h) {
+                const int j0 = 4 * (threadIdx.x + h * kPartThreads);
                 const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(in + j0);
                 const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(in + j0 + 2);
                 x[4 * h] = a.x; x[4 * h + 1] = a.y; x[4 * h + 2] = b.x; x[4 * h + 3] = b.y;
+            }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) r[4 * h + q] = 0;
-            } else {
+            for (int k = 0; k < kPartEPT; ++k) {
+                hi_or |= (unsigned)(x[k] >> 32);
+                r[k] = 0;
+            }
+            if constexpr (Src::kMaskRoute) {
+                if ((int)hi_or >= 0) {
+                    fast = true;
+                    const unsigned m = src.mask32();
+#pragma unroll
+                    for (int k = 0; k < kPartEPT; ++k) r[k] = (int)(((unsigned)x[k] & m) >> kPartShift);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j0 = 4 * (threadIdx.x + h * kPartThreads);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int j = j0 + q;
@@ -551,21 +575,16 @@ __global__ void __launch_bounds__(kPartThreads, 2)
                     x[4 * h + q] = j < have ? in[j] : (j < cnt ? src.raw1(e0 + j) : 0ULL);
                 }
             }
-        }
-        // high words of the present elements: a tile whose high words are all
-        // zero is staged as 4-byte records
-        unsigned hi_or = 0u;
 #pragma unroll
-        for (int k = 0; k < kPartEPT; ++k) hi_or |= r[k] == 0 ? (unsigned)(x[k] >> 32) : 0u;
-        bool fast = false;
-        if constexpr (Src::kMaskRoute) {
-            // all present elements non-negative: the bin is the masked low word
-            if ((int)hi_or >= 0) {
-                fast = true;
-                const unsigned m = src.mask32();
+            for (int k = 0; k < kPartEPT; ++k) hi_or |= r[k] == 0 ? (unsigned)(x[k] >> 32) : 0u;
+            if constexpr (Src::kMaskRoute) {
+                if ((int)hi_or >= 0) {
+                    fast = true;
+                    const unsigned m = src.mask32();
 #pragma unroll
-                for (int k = 0; k < kPartEPT; ++k)
-                    if (r[k] == 0) r[k] = (int)(((unsigned)x[k] & m) >> kPartShift);
+                    for (int k = 0; k < kPartEPT; ++k)
+                        if (r[k] == 0) r[k] = (int)(((unsigned)x[k] & m) >> kPartShift);
+                }
             }
         }
         if (!fast) {
@@ -581,14 +600,20 @@ __global__ void __launch_bounds__(kPartThreads, 2)
                 }
             }
         }
+        const bool clean = full && fast;
         // per-thread counts, two 16-bit fields per word (ranges 2w and 2w + 1)
         unsigned C[NW];
         if constexpr (NW == 2) {
             // up to four ranges: count in one word of 8-bit fields, then widen
             unsigned c8 = 0u;
+            if (clean) {
 #pragma unroll
-            for (int k = 0; k < kPartEPT; ++k)
-                if (r[k] >= 0) c8 += 1u << (r[k] << 3);
+                for (int k = 0; k < kPartEPT; ++k) c8 += 1u << (r[k] << 3);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kPartEPT; ++k)
+                    if (r[k] >= 0) c8 += 1u << (r[k] << 3);
+            }
             C[0] = (c8 & 0xffu) | ((c8 & 0xff00u) << 8);
             C[1] = ((c8 >> 16) & 0xffu) | ((c8 >> 8) & 0xff0000u);
         } else {
@@ -654,20 +679,28 @@ __global__ void __launch_bounds__(kPartThreads, 2)
 #pragma unroll
         for (int w = 0; w < NW; ++w) E[w] += wtot[w][warp];
         if constexpr (NW == 2) {
-            // this thread's first slot in each range, then a running byte count
-            const unsigned b0 = rstart[0] + (E[0] & 0xffffu), b1 = rstart[1] + (E[0] >> 16);
-            const unsigned b2 = rstart[2] + (E[1] & 0xffffu), b3 = rstart[3] + (E[1] >> 16);
-            unsigned run8 = 0u;
+            // this thread's next slot in each range, as a shared-memory cursor
+            // (cursor q of thread t at cur[q * kPartThreads + t]: conflict-free)
+            unsigned* cur = scur + threadIdx.x;
+            cur[0] = rstart[0] + (E[0] & 0xffffu);
+            cur[kPartThreads] = rstart[1] + (E[0] >> 16);
+            cur[2 * kPartThreads] = rstart[2] + (E[1] & 0xffffu);
+            cur[3 * kPartThreads] = rstart[3] + (E[1] >> 16);
+            unsigned* in32 = reinterpret_cast<unsigned*>(in);
+            auto place = [&](int k) {
+                unsigned* c = cur + r[k] * kPartThreads;
+                const unsigned p = *c;
+                *c = p + 1u;
+                if (wide) in[p] = x[k];
+                else in32[p] = (unsigned)x[k];
+            };
+            if (clean) {
 #pragma unroll
-            for (int k = 0; k < kPartEPT; ++k) {
-                if (r[k] >= 0) {
-                    const int s8 = r[k] << 3;
-                    const unsigned local = (run8 >> s8) & 0xffu;
-                    run8 += 1u << s8;
-                    const unsigned b = (r[k] & 2) ? ((r[k] & 1) ? b3 : b2) : ((r[k] & 1) ? b1 : b0);
-                    if (wide) in[b + local] = x[k];
-                    else reinterpret_cast<unsigned*>(in)[b + local] = (unsigned)x[k];
-                }
+                for (int k = 0; k < kPartEPT; ++k) place(k);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kPartEPT; ++k)
+                    if (r[k] >= 0) place(k);
             }
         } else {
 #pragma unroll
@@ -703,8 +736,8 @@ __global__ void __launch_bounds__(kPartThreads, 2)
             // the last partial 16 bytes
             unsigned char* dst = reinterpret_cast<unsigned char*>(staged + e0);
             const unsigned char* srcb = reinterpret_cast<const unsigned char*>(in);
-            for (unsigned b = sbytes; b < all; b += 4)
-                *reinterpret_cast<unsigned*>(dst + b) = *reinterpret_cast<const unsigned*>(srcb + b);
+            for (unsigned bb = sbytes; bb < all; bb += 4)
+                *reinterpret_cast<unsigned*>(dst + bb) = *reinterpret_cast<const unsigned*>(srcb + bb);
         }
         // run bounds; bit 15 marks a tile staged as 4-byte records
         if (threadIdx.x <= P)
@@ -1087,7 +1120,8 @@ static int launch_partition(const Src& src, int64_t n, long long bins, const His
             const int64_t ntiles = (m + kPartTile - 1) / kPartTile;
             Src part = src;
             part.data += off;
-            const unsigned g1 = (unsigned)(ntiles < 2LL * d->sm_count ? ntiles : 2LL * d->sm_count);
+            const int64_t g1max = (int64_t)kPartCtasPerSm * d->sm_count;
+            const unsigned g1 = (unsigned)(ntiles < g1max ? ntiles : g1max);
             stage_k<<<g1, kPartThreads, kPartStageSmem, stream>>>(part, m, bulk, bins, P, ntiles, staged,
                                                                  bounds, queue + 32, d->d_err);
             HYD_TRY(launch_check("weighted_histogram partition stage"));
