@@ -220,7 +220,7 @@ int hyd_cuda_autotune_stencil2d(int kind, int64_t h, int64_t w, int reps, int* b
     }
     cudaStream_t s = nullptr;
     int st = hyd_cuda_fill_uniform_f64(a, h * w, 99, 0.0, 1.0, s);
-    const int nvar = 7;
+    const int nvar = 21;  // 7 shapes x 3 integer-pipe levels
     double best_us = 1e300;
     int best_v = -1;
     for (int v = 0; v < nvar && st == HYD_CUDA_OK; ++v) {

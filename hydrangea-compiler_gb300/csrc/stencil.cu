@@ -39,15 +39,20 @@
 #include <map>
 #include <tuple>
 
+#include "fp64_emu.cuh"
 #include "hyd_common.cuh"
 
 namespace hyd {
 
 enum { ST_LAPLACIAN = 0, ST_JACOBI = 1, ST_HEAT = 2, ST_HEAT_EXAMPLE = 3 };
 
-template <int KIND>
+// EMU: how many of the three additions a + b, + c, + d run on the integer
+// pipe (dadd_pos, bit-identical to __dadd_rn); the rest use the FP64 unit.
+template <int KIND, int EMU>
 __device__ __forceinline__ double stencil_body(double a, double b, double c, double d, double e) {
-    const double t3 = __dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d);
+    const double t1 = EMU >= 1 ? dadd_pos(a, b) : __dadd_rn(a, b);
+    const double t2 = EMU >= 2 ? dadd_pos(t1, c) : __dadd_rn(t1, c);
+    const double t3 = EMU >= 3 ? dadd_pos(t2, d) : __dadd_rn(t2, d);
     if (KIND == ST_LAPLACIAN) return __fma_rn(e, -4.0, t3);
     if (KIND == ST_JACOBI) return __dmul_rn(t3, 0.25);
     if (KIND == ST_HEAT) {
@@ -58,7 +63,7 @@ __device__ __forceinline__ double stencil_body(double a, double b, double c, dou
 }
 
 // ---------------------------------------------------------------- plain path
-template <int KIND>
+template <int KIND, int EMU>
 __global__ void __launch_bounds__(256) stencil_plain_kernel(const double* __restrict__ in,
                                                             double* __restrict__ out, int64_t h,
                                                             int64_t w) {
@@ -67,7 +72,7 @@ __global__ void __launch_bounds__(256) stencil_plain_kernel(const double* __rest
     if (i >= h || j >= w) return;
     const int64_t im = i > 0 ? i - 1 : 0, ip = i + 1 < h ? i + 1 : h - 1;
     const int64_t jm = j > 0 ? j - 1 : 0, jp = j + 1 < w ? j + 1 : w - 1;
-    out[i * w + j] = stencil_body<KIND>(in[im * w + j], in[ip * w + j], in[i * w + jm],
+    out[i * w + j] = stencil_body<KIND, EMU>(in[im * w + j], in[ip * w + j], in[i * w + jm],
                                         in[i * w + jp], in[i * w + j]);
 }
 
@@ -100,7 +105,7 @@ __device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap* map
         : "memory");
 }
 
-template <int KIND, int kTH, int kTW>
+template <int KIND, int kTH, int kTW, int EMU>
 __global__ void __launch_bounds__(kStThreads)
     stencil_tma_kernel(const __grid_constant__ CUtensorMap in_map, double* __restrict__ out,
                        int h, int w, unsigned* err) {
@@ -167,7 +172,7 @@ __global__ void __launch_bounds__(kStThreads)
                 const double dn = sm[(r + 1) * kBoxW + c];
                 const double lf = sm[r * kBoxW + c - 1];
                 const double rt = sm[r * kBoxW + c + 1];
-                o[(int64_t)k * w] = stencil_body<KIND>(up, dn, lf, rt, mid);
+                o[(int64_t)k * w] = stencil_body<KIND, EMU>(up, dn, lf, rt, mid);
                 up = mid;
                 mid = dn;
             }
@@ -180,7 +185,7 @@ __global__ void __launch_bounds__(kStThreads)
                 if (i < h) {
                     const int im = (i > 0 ? i - 1 : 0) - i0 + 1, ip = (i + 1 < h ? i + 1 : h - 1) - i0 + 1;
                     const int ic = i - i0 + 1;
-                    out[(int64_t)i * w + j] = stencil_body<KIND>(sm[im * kBoxW + jc], sm[ip * kBoxW + jc],
+                    out[(int64_t)i * w + j] = stencil_body<KIND, EMU>(sm[im * kBoxW + jc], sm[ip * kBoxW + jc],
                                                                  sm[ic * kBoxW + jm], sm[ic * kBoxW + jp],
                                                                  sm[ic * kBoxW + jc]);
                 }
@@ -233,20 +238,28 @@ static int make_map(CUtensorMap* map, const double* p, int64_t h, int64_t w, int
     return HYD_CUDA_OK;
 }
 
-// Tile variants (index = the autotuner's choice): 0 is the reference's fixed
-// 32 x 32 polyhedral tile (Polyhedral.hs:196-204), the others GPU-shaped.
+// Variants (index = the autotuner's choice) = shape + kShapes * level.
+// Shapes: 0 is the reference's fixed 32 x 32 polyhedral tile
+// (Polyhedral.hs:196-204), 1-5 GPU-shaped TMA tiles, 6 the plain kernel.
+// Levels: how many of the three sum additions run on the integer pipe
+// (kEmuLevels[level]); every variant gives bit-identical results.
 struct TileVariant {
     int th, tw;
 };
 static const TileVariant kTiles[] = {{32, 32}, {16, 128}, {16, 64}, {32, 64}, {8, 128}, {32, 128}};
 constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
-constexpr int kPlainVariant = kNumTiles;  // the non-TMA kernel
-constexpr int kDefaultTile = 1;           // 16 x 128
+constexpr int kShapes = kNumTiles + 1;     // + the plain (non-TMA) kernel
+constexpr int kPlainShape = kNumTiles;
+constexpr int kEmuLevels[] = {0, 2, 3};
+constexpr int kNumLevels = sizeof(kEmuLevels) / sizeof(kEmuLevels[0]);
+constexpr int kNumVariants = kShapes * kNumLevels;
+constexpr int kDefaultVariant = kPlainShape + kShapes;  // plain kernel, 2 integer-pipe sums
+                                                        // (fastest at 8192^2 heat on GB300)
 
-template <int KIND, int TH, int TW>
+template <int KIND, int TH, int TW, int EMU>
 static int launch_tma(const CUtensorMap* map, double* out, int64_t h, int64_t w, const Device* d, cudaStream_t stream) {
     using S = TileShape<TH, TW>;
-    auto k = stencil_tma_kernel<KIND, TH, TW>;
+    auto k = stencil_tma_kernel<KIND, TH, TW, EMU>;
     HYD_TRY(configure_kernel((const void*)k, d, false));
     const int64_t ntiles = ((h + TH - 1) / TH) * ((w + TW - 1) / TW);
     int occ = 0;
@@ -258,22 +271,33 @@ static int launch_tma(const CUtensorMap* map, double* out, int64_t h, int64_t w,
     return HYD_CUDA_OK;
 }
 
-template <int KIND>
-static int launch_step_kind(const CUtensorMap* map, const double* in, double* out, int64_t h, int64_t w,
-                            int variant, const Device* d, cudaStream_t stream) {
-    switch (variant) {
-        case 0: HYD_TRY((launch_tma<KIND, 32, 32>(map, out, h, w, d, stream))); break;
-        case 1: HYD_TRY((launch_tma<KIND, 16, 128>(map, out, h, w, d, stream))); break;
-        case 2: HYD_TRY((launch_tma<KIND, 16, 64>(map, out, h, w, d, stream))); break;
-        case 3: HYD_TRY((launch_tma<KIND, 32, 64>(map, out, h, w, d, stream))); break;
-        case 4: HYD_TRY((launch_tma<KIND, 8, 128>(map, out, h, w, d, stream))); break;
-        case 5: HYD_TRY((launch_tma<KIND, 32, 128>(map, out, h, w, d, stream))); break;
+template <int KIND, int EMU>
+static int launch_shape(const CUtensorMap* map, const double* in, double* out, int64_t h, int64_t w, int shape,
+                        const Device* d, cudaStream_t stream) {
+    switch (shape) {
+        case 0: HYD_TRY((launch_tma<KIND, 32, 32, EMU>(map, out, h, w, d, stream))); break;
+        case 1: HYD_TRY((launch_tma<KIND, 16, 128, EMU>(map, out, h, w, d, stream))); break;
+        case 2: HYD_TRY((launch_tma<KIND, 16, 64, EMU>(map, out, h, w, d, stream))); break;
+        case 3: HYD_TRY((launch_tma<KIND, 32, 64, EMU>(map, out, h, w, d, stream))); break;
+        case 4: HYD_TRY((launch_tma<KIND, 8, 128, EMU>(map, out, h, w, d, stream))); break;
+        case 5: HYD_TRY((launch_tma<KIND, 32, 128, EMU>(map, out, h, w, d, stream))); break;
         default: {
             dim3 grid((unsigned)((w + 31) / 32), (unsigned)((h + 7) / 8));
-            stencil_plain_kernel<KIND><<<grid, 256, 0, stream>>>(in, out, h, w);
+            stencil_plain_kernel<KIND, EMU><<<grid, 256, 0, stream>>>(in, out, h, w);
         }
     }
     return launch_check("stencil2d_f64");
+}
+
+template <int KIND>
+static int launch_step_kind(const CUtensorMap* map, const double* in, double* out, int64_t h, int64_t w,
+                            int variant, const Device* d, cudaStream_t stream) {
+    const int shape = variant % kShapes;
+    switch (kEmuLevels[variant / kShapes]) {
+        case 2: return launch_shape<KIND, 2>(map, in, out, h, w, shape, d, stream);
+        case 3: return launch_shape<KIND, 3>(map, in, out, h, w, shape, d, stream);
+        default: return launch_shape<KIND, 0>(map, in, out, h, w, shape, d, stream);
+    }
 }
 
 static int launch_step(int kind, const CUtensorMap* map, const double* in, double* out, int64_t h, int64_t w,
@@ -289,16 +313,22 @@ static int launch_step(int kind, const CUtensorMap* map, const double* in, doubl
 // Variant for (kind, h, w): the autotuner's cached choice, else the default;
 // shapes TMA cannot describe always take the plain kernel.
 static int choose_variant(int kind, const double* a, const double* b, int64_t h, int64_t w, int forced) {
+    int v = kDefaultVariant;
+    if (forced >= 0 && forced < kNumVariants) {
+        v = forced;
+    } else {
+        const int t = tune_lookup_stencil(kind, h, w);
+        if (t >= 0 && t < kNumVariants) v = t;
+    }
     const bool tma = tma_ok(a, h, w) && (b == nullptr || tma_ok(b, h, w));
-    if (!tma) return kPlainVariant;
-    if (forced >= 0 && forced <= kPlainVariant) return forced;
-    const int t = tune_lookup_stencil(kind, h, w);
-    return t >= 0 && t <= kPlainVariant ? t : kDefaultTile;
+    if (!tma) v = (v / kShapes) * kShapes + kPlainShape;  // same level, plain kernel
+    return v;
 }
 
 static int maps_for(int variant, const double* p, int64_t h, int64_t w, CUtensorMap* map) {
-    if (variant >= kNumTiles) return HYD_CUDA_OK;
-    return make_map(map, p, h, w, kTiles[variant].tw + 4, kTiles[variant].th + 2);
+    const int shape = variant % kShapes;
+    if (shape >= kNumTiles) return HYD_CUDA_OK;
+    return make_map(map, p, h, w, kTiles[shape].tw + 4, kTiles[shape].th + 2);
 }
 
 // Cached executable graphs of whole `iterate` runs.
@@ -324,7 +354,7 @@ extern "C" int hyd_cuda_stencil2d_f64_variant(int kind, const double* in, double
     HYD_CHECK_ARG(h >= 0 && w >= 0, "stencil2d: negative shape");
     HYD_CHECK_ARG(h * w == 0 || (in != nullptr && out != nullptr), "stencil2d: null buffer");
     HYD_CHECK_ARG(in != out || h * w == 0, "stencil2d: input and output must differ");
-    HYD_CHECK_ARG(variant >= -1 && variant <= kPlainVariant, "stencil2d: unknown variant %d", variant);
+    HYD_CHECK_ARG(variant >= -1 && variant < kNumVariants, "stencil2d: unknown variant %d", variant);
     if (h == 0 || w == 0) return HYD_CUDA_OK;
     Device* d = nullptr;
     HYD_TRY(device(&d));
@@ -346,7 +376,7 @@ extern "C" int hyd_cuda_iterate_stencil2d_f64_variant(int kind, double* buf0, do
     HYD_CHECK_ARG(final_buf != nullptr, "iterate_stencil2d: null final_buf");
     HYD_CHECK_ARG(h * w == 0 || (buf0 != nullptr && buf1 != nullptr && buf0 != buf1),
                   "iterate_stencil2d: need two distinct buffers");
-    HYD_CHECK_ARG(variant >= -1 && variant <= kPlainVariant, "iterate_stencil2d: unknown variant %d", variant);
+    HYD_CHECK_ARG(variant >= -1 && variant < kNumVariants, "iterate_stencil2d: unknown variant %d", variant);
     *final_buf = (int)(iters & 1);
     if (h == 0 || w == 0 || iters == 0) return HYD_CUDA_OK;
     Device* d = nullptr;
@@ -363,7 +393,7 @@ extern "C" int hyd_cuda_iterate_stencil2d_f64_variant(int kind, double* buf0, do
             HYD_TRY(launch_step(kind, &maps[t & 1], bufs[t & 1], bufs[(t + 1) & 1], h, w, v, d, st));
         return HYD_CUDA_OK;
     }
-    GraphKey key{kind * 16 + v, h, w, iters, buf0, buf1, st};
+    GraphKey key{kind * 256 + v, h, w, iters, buf0, buf1, st};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_graph_mu);
@@ -408,4 +438,27 @@ extern "C" void hyd_cuda_stencil_release_graphs(void) {
     std::lock_guard<std::mutex> lock(g_graph_mu);
     for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
     g_graphs.clear();
+}
+
+// ---------------------------------------------------------------- self-test
+namespace hyd {
+__global__ void dadd_selftest_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                                     double* __restrict__ emu, double* __restrict__ hw, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        emu[i] = dadd_pos(x[i], y[i]);
+        hw[i] = __dadd_rn(x[i], y[i]);
+    }
+}
+}  // namespace hyd
+
+extern "C" int hyd_cuda_selftest_dadd(const double* x, const double* y, double* emu, double* hw, int64_t n,
+                                      void* stream) {
+    HYD_CHECK_ARG(n >= 0 && (n == 0 || (x && y && emu && hw)), "selftest_dadd: bad arguments");
+    if (n == 0) return HYD_CUDA_OK;
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    const int64_t want = (n + 255) / 256;
+    const unsigned grid = (unsigned)(want < (int64_t)d->sm_count * 8 ? want : (int64_t)d->sm_count * 8);
+    dadd_selftest_kernel<<<grid, 256, 0, as_stream(stream)>>>(x, y, emu, hw, n);
+    return launch_check("selftest_dadd");
 }

@@ -50,6 +50,7 @@ SIGNATURES = {
     "hyd_cuda_iterate_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _i64, C.POINTER(C.c_int), _p]),
     "hyd_cuda_stencil_release_graphs": (None, []),
     "hyd_cuda_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i, _p]),
+    "hyd_cuda_selftest_dadd": (_i, [_p, _p, _p, _p, _i64, _p]),
     "hyd_cuda_iterate_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i64, _i, C.POINTER(C.c_int), _p]),
     "hyd_cuda_tune_cache_path": (C.c_char_p, []),
     "hyd_cuda_tune_set_cache_path": (_i, [C.c_char_p]),
@@ -237,7 +238,10 @@ def scatter_add_f64(idx, vals, dst, stream=None):
          stream_handle(stream))
 
 
-STENCIL_VARIANTS = {0: (32, 32), 1: (16, 128), 2: (16, 64), 3: (32, 64), 4: (8, 128), 5: (32, 128), 6: "plain"}
+_STENCIL_SHAPES = [(32, 32), (16, 128), (16, 64), (32, 64), (8, 128), (32, 128), "plain"]
+_STENCIL_EMU = [0, 2, 3]  # sum additions on the integer pipe, per level
+STENCIL_VARIANTS = {s + 7 * l: (_STENCIL_SHAPES[s] if l == 0 else (_STENCIL_SHAPES[s], "int-add x%d" % _STENCIL_EMU[l]))
+                    for l in range(3) for s in range(7)}
 
 
 def stencil2d(kind, src, dst, stream=None, variant=-1):
@@ -254,10 +258,18 @@ def iterate_stencil2d(kind, buf0, buf1, iters, stream=None, variant=-1):
     return buf0 if fb.value == 0 else buf1
 
 
+def selftest_dadd(x, y):
+    """(integer-pipe sums, FP64-unit sums) of two float64 device tensors."""
+    import torch
+    emu, hw = torch.empty_like(x), torch.empty_like(x)
+    call("hyd_cuda_selftest_dadd", ptr(x), ptr(y), ptr(emu), ptr(hw), x.numel(), None)
+    return emu, hw
+
+
 def autotune_stencil2d(kind, h, w, reps=5):
     import numpy as np
     best = C.c_int(-1)
-    times = np.zeros(7)
+    times = np.zeros(len(STENCIL_VARIANTS))
     call("hyd_cuda_autotune_stencil2d", kind, h, w, reps, C.byref(best), times.ctypes.data)
     return best.value, times
 

@@ -163,13 +163,21 @@ int hyd_cuda_stencil2d_f64(int kind, const double* in, double* out, int64_t h, i
  * iters, stream) and replayed on later calls. */
 int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
                                    int64_t iters, int* final_buf, void* stream);
+/* Self-test of the integer-pipe binary64 addition the stencil variants of
+ * levels 1-2 use: emu[i] = that addition of x[i] and y[i], hw[i] = the FP64
+ * unit's x[i] + y[i] (round to nearest even).  No counterpart in the
+ * reference; for tests. */
+int hyd_cuda_selftest_dadd(const double* x, const double* y, double* emu, double* hw, int64_t n, void* stream);
 /* Releases the cached iterate graphs (also done by hyd_cuda_cleanup). */
 void hyd_cuda_stencil_release_graphs(void);
-/* Same, with an explicit kernel variant instead of the autotuned one: 0..5 are
+/* Same, with an explicit kernel variant instead of the autotuned one
+ * (-1 = autotuned/default).  variant = shape + 7 * level.  Shapes 0..5 are
  * TMA tile shapes (0 = 32x32, the reference's fixed polyhedral tile,
  * Polyhedral.hs:196-204; 1 = 16x128, 2 = 16x64, 3 = 32x64, 4 = 8x128,
- * 5 = 32x128), 6 = the plain non-TMA kernel, -1 = autotuned/default.  All
- * variants give identical bits. */
+ * 5 = 32x128), 6 = the plain non-TMA kernel.  Levels 0, 1, 2 run 0, 2, 3 of
+ * the three additions of the 4-neighbour sum on the integer pipe (exact
+ * round-to-nearest-even; FP64 is the scarce pipe on GB300).  All 21 variants
+ * give identical bits. */
 int hyd_cuda_stencil2d_f64_variant(int kind, const double* in, double* out, int64_t h, int64_t w,
                                    int variant, void* stream);
 int hyd_cuda_iterate_stencil2d_f64_variant(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
@@ -186,7 +194,7 @@ const char* hyd_cuda_tune_cache_path(void);
 int hyd_cuda_tune_set_cache_path(const char* path);     /* reloads the table from `path` */
 int hyd_cuda_tune_record(const char* device, const char* kernel, const char* klass, int choice, double us);
 int hyd_cuda_tune_query(const char* device, const char* kernel, const char* klass);  /* -1 if absent */
-/* Time every stencil variant (times_us[7], may be NULL) / histogram strategy
+/* Time every stencil variant (times_us[21], may be NULL) / histogram strategy
  * (times_us[6], index = strategy, -1 when it cannot run) on scratch inputs and
  * record the fastest in *best. */
 int hyd_cuda_autotune_stencil2d(int kind, int64_t h, int64_t w, int reps, int* best, double* times_us);
