@@ -198,7 +198,8 @@ __global__ void __launch_bounds__(kBatchThreads) batch_scatter_kernel(const Batc
                                                                       const WorkItem* __restrict__ items,
                                                                       unsigned nitems, unsigned* cursor,
                                                                       const long long* __restrict__ row_start,
-                                                                      unsigned* __restrict__ counts) {
+                                                                      unsigned* __restrict__ counts,
+                                                                      unsigned* __restrict__ coo_idx) {
     unsigned it;
     while (next_item(cursor, nitems, it)) {
         const WorkItem w = items[it];
@@ -213,14 +214,16 @@ __global__ void __launch_bounds__(kBatchThreads) batch_scatter_kernel(const Batc
             const long long slot = row_start[g] - I.scan_base + (long long)left - 1;
             I.csr_cols[slot] = c;
             I.csr_vals[slot] = I.vals[k];
+            coo_idx[I.scan_base + slot] = (unsigned)k;  // orders equal columns in stage 4
         }
     }
 }
 
-// Warp-wide bitonic sort of up to 32*kPer (col, val) pairs held kPer per lane
-// in "lane-major" order (element j*32 + lane in slot j).  Padding uses INT_MAX.
-template <int kPer>
-__device__ __forceinline__ void warp_bitonic_sort(int (&key)[kPer], double (&val)[kPer]) {
+// Warp-wide bitonic sort of up to 32*kPer (key, val) pairs held kPer per lane
+// in "lane-major" order (element j*32 + lane in slot j).  Padding uses the
+// largest key.
+template <int kPer, class K>
+__device__ __forceinline__ void warp_bitonic_sort(K (&key)[kPer], double (&val)[kPer]) {
     const int lane = threadIdx.x & 31;
     constexpr int N = 32 * kPer;
 #pragma unroll
@@ -238,7 +241,7 @@ __device__ __forceinline__ void warp_bitonic_sort(int (&key)[kPer], double (&val
                         const int jj = j + sj;
                         const bool swap = up ? (key[j] > key[jj]) : (key[j] < key[jj]);
                         if (swap) {
-                            int tk = key[j]; key[j] = key[jj]; key[jj] = tk;
+                            const K tk = key[j]; key[j] = key[jj]; key[jj] = tk;
                             double tv = val[j]; val[j] = val[jj]; val[jj] = tv;
                         }
                     }
@@ -247,7 +250,7 @@ __device__ __forceinline__ void warp_bitonic_sort(int (&key)[kPer], double (&val
 #pragma unroll
                 for (int j = 0; j < kPer; ++j) {
                     const int idx = j * 32 + lane;
-                    const int ok = __shfl_xor_sync(0xffffffffu, key[j], stride);
+                    const K ok = __shfl_xor_sync(0xffffffffu, key[j], stride);
                     const double ov = __shfl_xor_sync(0xffffffffu, val[j], stride);
                     const bool up = (idx & size) == 0;
                     const bool lower = (lane & stride) == 0;
@@ -263,16 +266,19 @@ __device__ __forceinline__ void warp_bitonic_sort(int (&key)[kPer], double (&val
     }
 }
 
+// Sort key: column, then COO position -- the runtime's stable order for equal
+// (row, col) entries.
 template <int kPer>
-__device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* __restrict__ cv, int len,
+__device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* __restrict__ cv,
+                                                  const unsigned* __restrict__ coo_idx, int len,
                                                   const double* __restrict__ x, double* yrow) {
     const int lane = threadIdx.x & 31;
-    int key[kPer];
+    long long key[kPer];
     double val[kPer];
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
         const int i = j * 32 + lane;
-        key[j] = i < len ? cc[i] : 0x7fffffff;
+        key[j] = i < len ? (((long long)cc[i] << 32) | coo_idx[i]) : 0x7fffffffffffffffLL;
         val[j] = i < len ? cv[i] : 0.0;
     }
     warp_bitonic_sort<kPer>(key, val);
@@ -281,9 +287,10 @@ __device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* 
     for (int j = 0; j < kPer; ++j) {
         const int i = j * 32 + lane;
         if (i < len) {
-            cc[i] = key[j];
+            const int c = (int)(key[j] >> 32);
+            cc[i] = c;
             cv[i] = val[j];
-            acc = fma(val[j], x[key[j]], acc);
+            acc = fma(val[j], x[c], acc);
         }
     }
 #pragma unroll
@@ -295,7 +302,7 @@ __device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* 
 // Also writes the instance's row_ptr (relative to its entry base).
 __global__ void __launch_bounds__(kBatchThreads) batch_sort_spmv_kernel(
     const BatchInst* __restrict__ inst, const WorkItem* __restrict__ items, unsigned nitems, unsigned* cursor,
-    const long long* __restrict__ row_start, unsigned* err) {
+    const long long* __restrict__ row_start, const unsigned* __restrict__ coo_idx, unsigned* err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int W = kBatchThreads / 32;
     unsigned it;
@@ -316,10 +323,11 @@ __global__ void __launch_bounds__(kBatchThreads) batch_sort_spmv_kernel(
             }
             int* cc = I.csr_cols + s;
             double* cv = I.csr_vals + s;
-            if (len <= 32) sort_row_and_spmv<1>(cc, cv, len, I.x, I.y + r);
-            else if (len <= 64) sort_row_and_spmv<2>(cc, cv, len, I.x, I.y + r);
-            else if (len <= 128) sort_row_and_spmv<4>(cc, cv, len, I.x, I.y + r);
-            else if (len <= 256) sort_row_and_spmv<8>(cc, cv, len, I.x, I.y + r);
+            const unsigned* ci = coo_idx + I.scan_base + s;
+            if (len <= 32) sort_row_and_spmv<1>(cc, cv, ci, len, I.x, I.y + r);
+            else if (len <= 64) sort_row_and_spmv<2>(cc, cv, ci, len, I.x, I.y + r);
+            else if (len <= 128) sort_row_and_spmv<4>(cc, cv, ci, len, I.x, I.y + r);
+            else if (len <= 256) sort_row_and_spmv<8>(cc, cv, ci, len, I.x, I.y + r);
             else bad = true;  // rows above 256 entries are outside this kernel's contract
         }
     }
@@ -349,13 +357,17 @@ int batch_pipeline_rows(std::vector<BatchInst>& inst, const char* key, cudaStrea
         entries += I.nnz;
     }
     if (rows_total >= (1LL << 32)) return set_error(HYD_CUDA_ERR_UNSUPPORTED, "batch: too many rows");
+    for (const BatchInst& I : inst)  // COO positions are kept as 32-bit indices
+        if (I.nnz > (1LL << 32)) return set_error(HYD_CUDA_ERR_UNSUPPORTED, "batch: instance above 2^32 entries");
     const size_t inst_bytes = (inst.size() * sizeof(BatchInst) + 255) & ~(size_t)255;
     const size_t ci_bytes = ((count_items.size() * sizeof(WorkItem)) + 255) & ~(size_t)255;
     const size_t ri_bytes = ((row_items.size() * sizeof(WorkItem)) + 255) & ~(size_t)255;
     const size_t cnt_bytes = ((size_t)rows_total * 4 + 255) & ~(size_t)255;
     const size_t wide_bytes = ((size_t)rows_total * 8 + 255) & ~(size_t)255;
     void* buf = nullptr;
-    HYD_TRY(device_buffer(d, key, inst_bytes + ci_bytes + ri_bytes + cnt_bytes + 2 * wide_bytes + 256, &buf));
+    const size_t idx_bytes = ((size_t)entries * 4 + 255) & ~(size_t)255;
+    HYD_TRY(device_buffer(d, key, inst_bytes + ci_bytes + ri_bytes + cnt_bytes + 2 * wide_bytes + 256 + idx_bytes,
+                          &buf));
     unsigned char* b = static_cast<unsigned char*>(buf);
     BatchInst* d_inst = reinterpret_cast<BatchInst*>(b);
     WorkItem* d_ci = reinterpret_cast<WorkItem*>(b + inst_bytes);
@@ -364,6 +376,7 @@ int batch_pipeline_rows(std::vector<BatchInst>& inst, const char* key, cudaStrea
     long long* wide = reinterpret_cast<long long*>(b + inst_bytes + ci_bytes + ri_bytes + cnt_bytes);
     long long* row_start = wide + (wide_bytes / 8);
     unsigned* cursors = reinterpret_cast<unsigned*>(b + inst_bytes + ci_bytes + ri_bytes + cnt_bytes + 2 * wide_bytes);
+    unsigned* coo_idx = reinterpret_cast<unsigned*>(b + inst_bytes + ci_bytes + ri_bytes + cnt_bytes + 2 * wide_bytes + 256);
     const size_t table_bytes = inst_bytes + ci_bytes + ri_bytes;
     const unsigned char* src_inst = reinterpret_cast<const unsigned char*>(inst.data());
     const unsigned char* src_ci = reinterpret_cast<const unsigned char*>(count_items.data());
@@ -394,11 +407,11 @@ int batch_pipeline_rows(std::vector<BatchInst>& inst, const char* key, cudaStrea
     HYD_TRY(scan_i64_launch(wide, row_start, rows_total, 0, false, false, s));
     if (!count_items.empty()) {
         batch_scatter_kernel<<<grid, kBatchThreads, 0, s>>>(d_inst, d_ci, (unsigned)count_items.size(), cursors + 1,
-                                                            row_start, counts);
+                                                            row_start, counts, coo_idx);
         HYD_TRY(launch_check("batch_scatter"));
     }
     batch_sort_spmv_kernel<<<grid, kBatchThreads, 0, s>>>(d_inst, d_ri, (unsigned)row_items.size(), cursors + 2,
-                                                          row_start, d->d_err);
+                                                          row_start, coo_idx, d->d_err);
     HYD_TRY(launch_check("batch_sort_spmv"));
     // pageable tables die with the caller's vectors: the copies must have run
     if (!async_tables) HYD_CUDA_TRY(cudaStreamSynchronize(s));

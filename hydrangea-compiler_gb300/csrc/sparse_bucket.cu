@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kBkThreads) bk_split_kernel(const BkInst* __re
                                                               const BkItem* __restrict__ items, unsigned nitems,
                                                               unsigned* cursor, const long long* __restrict__ bstart,
                                                               unsigned* __restrict__ bfill,
-                                                              unsigned* __restrict__ keys_out,
+                                                              uint2* __restrict__ keys_out,
                                                               double* __restrict__ vals_out) {
     __shared__ unsigned hist[kMaxSmemBuckets];
     __shared__ unsigned gbase[kMaxSmemBuckets];  // batch-wide slots (< 2^32, checked on the host)
@@ -158,7 +158,8 @@ __global__ void __launch_bounds__(kBkThreads) bk_split_kernel(const BkInst* __re
             const long long pos = smem ? (long long)gbase[bucket[j]] + rank[j]
                                        : bstart[I.bucket_base + bucket[j]] +
                                              atomicAdd(&bfill[I.bucket_base + bucket[j]], 1u);
-            keys_out[pos] = key[j];
+            // the key and the entry's COO position (orders equal (row, col) keys)
+            keys_out[pos] = make_uint2(key[j], (unsigned)k);
             vals_out[pos] = I.vals[k];
         }
         __syncthreads();
@@ -173,17 +174,42 @@ constexpr int kBkRounds = kBkSmallCap / kBkSmallThreads;  // 32-element rounds p
 // two (key, index) buffers, per-(warp, digit) counts, digit bases
 constexpr size_t kBkSmallSmem = (size_t)kBkSmallCap * 12 + (size_t)kBkSmallWarps * 256 * 4 + 256 * 4;
 
-// Fast path: a stable LSD radix sort of the bucket's keys (row << 24 | col) in
-// shared memory, 8-bit digits over the column bits then one pass on the row
-// digit; each warp owns 256 consecutive positions, ranked in rounds of 32 with
-// __match_any_sync so equal digits keep their order.  The last pass's digit
-// bases are the row offsets.  Then CSR columns/values are written in sorted
+// Equal (row, col) keys must keep their COO order (the runtime's stable
+// sort_indices).  The split's order inside a bucket is arbitrary, so after the
+// sort every run of equal keys is put in COO-position order (insertion sort
+// by the thread that owns the run's first slot; duplicates are rare).
+template <class IdxT>
+__device__ __forceinline__ void bk_order_equal_keys(const unsigned* key, IdxT* pos, int E,
+                                                    const uint2* __restrict__ rec) {
+    for (int p = threadIdx.x; p + 1 < E; p += blockDim.x) {
+        if (key[p + 1] != key[p] || (p > 0 && key[p - 1] == key[p])) continue;
+        int q = p + 2;
+        while (q < E && key[q] == key[p]) ++q;
+        for (int i = p + 1; i < q; ++i) {
+            const IdxT v = pos[i];
+            const unsigned kv = rec[v].y;  // COO position
+            int j = i - 1;
+            while (j >= p && rec[pos[j]].y > kv) {
+                pos[j + 1] = pos[j];
+                --j;
+            }
+            pos[j + 1] = v;
+        }
+    }
+}
+
+// Fast path: a stable LSD radix sort of the bucket's keys (row_in_bucket <<
+// cbits | col, 6 + cbits bits, 8 per pass) in shared memory; each warp owns
+// consecutive positions, ranked in rounds of 32 with __match_any_sync so equal
+// digits keep their order.  Row starts come from the row changes of the sorted
+// keys.  Then CSR columns/values are written in sorted
 // order (values gathered by index), and each warp computes the SpMV of its
 // rows with lane i summing sorted positions i, i+32, ... (the same order as the
 // other kernels).  Buckets above kBkSmallCap go to `overflow`.
-__global__ void __launch_bounds__(kBkSmallThreads) bk_bucket_small_kernel(
+constexpr int kBkSmallPerSm = 6;  // resident CTAs per SM
+__global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_small_kernel(
     const BkInst* __restrict__ inst, const BkItem* __restrict__ items, unsigned nitems, unsigned* cursor,
-    const long long* __restrict__ bstart, const unsigned* __restrict__ bcount, const unsigned* __restrict__ keys_in,
+    const long long* __restrict__ bstart, const unsigned* __restrict__ bcount, const uint2* __restrict__ keys_in,
     const double* __restrict__ vals_in, BkItem* __restrict__ overflow, unsigned* overflow_count, unsigned* err) {
     extern __shared__ __align__(16) unsigned char bks_smem[];
     unsigned* kbuf0 = reinterpret_cast<unsigned*>(bks_smem);
@@ -210,24 +236,26 @@ __global__ void __launch_bounds__(kBkSmallThreads) bk_bucket_small_kernel(
         const long long e0 = s0 - I.scan_base;
         const long long r0 = (long long)w.tile << kBkShift;
         const int nr = (int)((I.nrows - r0) < kBkRows ? (I.nrows - r0) : kBkRows);
+        int cbits = 0;
+        while ((1LL << cbits) < I.ncols) ++cbits;
+        // key = row_in_bucket << cbits | col: 6 + cbits bits, 8 per pass
+        const int passes = (kBkShift + cbits + 7) / 8;
         for (int i = threadIdx.x; i < E; i += kBkSmallThreads) {
-            kbuf0[i] = keys_in[s0 + i];
+            const unsigned k = keys_in[s0 + i].x;
+            kbuf0[i] = ((k >> 24) << cbits) | (k & 0xFFFFFFu);
             ibuf0[i] = (unsigned short)i;
         }
         // positions split evenly over the warps (whole 32-element rounds); warp
         // order is position order, so ranks stay stable
         const int chunk = (((E + kBkSmallWarps - 1) / kBkSmallWarps) + 31) & ~31;
         const int rounds = chunk / 32;
-        int cbits = 0;
-        while ((1LL << cbits) < I.ncols) ++cbits;
-        const int col_passes = (cbits + 7) / 8;
         unsigned* kin = kbuf0;
         unsigned* kout = kbuf1;
         unsigned short* iin = ibuf0;
         unsigned short* iout = ibuf1;
         __syncthreads();
-        for (int pass = 0; pass <= col_passes; ++pass) {
-            const int shift = pass < col_passes ? 8 * pass : 24;  // last pass: the row digit
+        for (int pass = 0; pass < passes; ++pass) {
+            const int shift = 8 * pass;
             for (int i = threadIdx.x; i < kBkSmallWarps * 256; i += kBkSmallThreads) wcount[i] = 0u;
             __syncthreads();
             unsigned rk[kBkRounds];
@@ -287,9 +315,17 @@ __global__ void __launch_bounds__(kBkSmallThreads) bk_bucket_small_kernel(
             unsigned* tk = kin; kin = kout; kout = tk;
             unsigned short* ti = iin; iin = iout; iout = ti;
         }
-        // kin/iin: sorted by (row, col); dbase[r] = first position of row r
+        // kin/iin: sorted by (row, col); row starts from the row changes
+        const unsigned cmask = (1u << cbits) - 1u;
+        for (int p = threadIdx.x; p <= E; p += kBkSmallThreads) {
+            const int rp = p == 0 ? -1 : (int)(kin[p - 1] >> cbits);
+            const int rc = p == E ? kBkRows : (int)(kin[p] >> cbits);
+            for (int r = rp + 1; r <= rc && r < kBkRows; ++r) dbase[r] = (unsigned)p;
+        }
+        bk_order_equal_keys(kin, iin, E, keys_in + s0);
+        __syncthreads();
         for (int p = threadIdx.x; p < E; p += kBkSmallThreads) {
-            I.csr_cols[e0 + p] = (int)(kin[p] & 0xFFFFFFu);
+            I.csr_cols[e0 + p] = (int)(kin[p] & cmask);
             I.csr_vals[e0 + p] = vals_in[s0 + iin[p]];
         }
         for (int r = threadIdx.x; r <= nr; r += kBkSmallThreads) {
@@ -302,7 +338,7 @@ __global__ void __launch_bounds__(kBkSmallThreads) bk_bucket_small_kernel(
             if (bb - a > 256) bad = true;  // a row above 256 entries: outside the contract
             double acc = 0.0;
             for (int p = a + lane; p < bb; p += 32)
-                acc = fma(vals_in[s0 + iin[p]], I.x[kin[p] & 0xFFFFFFu], acc);
+                acc = fma(vals_in[s0 + iin[p]], I.x[kin[p] & cmask], acc);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) I.y[r0 + r] = acc;
@@ -322,7 +358,7 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
                                                                const unsigned* nitems_dev, unsigned* cursor,
                                                                const long long* __restrict__ bstart,
                                                                const unsigned* __restrict__ bcount,
-                                                               const unsigned* __restrict__ keys_in,
+                                                               const uint2* __restrict__ keys_in,
                                                                const double* __restrict__ vals_in, unsigned* err) {
     extern __shared__ __align__(16) unsigned char bk_smem[];
     unsigned* key = reinterpret_cast<unsigned*>(bk_smem);
@@ -348,7 +384,7 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
         int P = 1;
         while (P < E) P <<= 1;
         for (int i = threadIdx.x; i < P; i += kBkThreads) {
-            key[i] = i < E ? keys_in[s0 + i] : 0xFFFFFFFFu;
+            key[i] = i < E ? keys_in[s0 + i].x : 0xFFFFFFFFu;
             idx[i] = (unsigned short)i;
         }
         __syncthreads();
@@ -375,6 +411,7 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
             const int rc = p == E ? nr : (int)(key[p] >> 24);
             for (int r = rp + 1; r <= rc && r <= nr; ++r) rstart[r] = p;
         }
+        bk_order_equal_keys(key, idx, E, keys_in + s0);  // the bitonic network is not stable
         __syncthreads();
         for (int p = threadIdx.x; p < E; p += kBkThreads) {
             I.csr_cols[e0 + p] = (int)(key[p] & 0xFFFFFFu);
@@ -434,9 +471,10 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     const size_t inst_b = al(inst.size() * sizeof(BkInst)), tiles_b = al(tiles.size() * sizeof(BkItem)),
                  bk_b = al(buckets.size() * sizeof(BkItem));
     const size_t cnt_b = al((size_t)nb_total * 4), wide_b = al((size_t)nb_total * 8);
-    const size_t keys_b = al((size_t)entries * 4), vals_b = al((size_t)entries * 8);
+    const size_t vals_b = al((size_t)entries * 8);
     void* buf = nullptr;
-    HYD_TRY(device_buffer(d, key, inst_b + tiles_b + 2 * bk_b + 2 * cnt_b + 2 * wide_b + keys_b + vals_b + 256, &buf));
+    HYD_TRY(device_buffer(d, key, inst_b + tiles_b + 2 * bk_b + 2 * cnt_b + 2 * wide_b + vals_b + vals_b + 256,
+                          &buf));
     unsigned char* b = static_cast<unsigned char*>(buf);
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -451,7 +489,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     unsigned* bfill = reinterpret_cast<unsigned*>(take(cnt_b));
     long long* wide = reinterpret_cast<long long*>(take(wide_b));
     long long* bstart = reinterpret_cast<long long*>(take(wide_b));
-    unsigned* keys = reinterpret_cast<unsigned*>(take(keys_b));
+    uint2* keys = reinterpret_cast<uint2*>(take(vals_b));  // (key, COO position) per entry
     double* vals = reinterpret_cast<double*>(take(vals_b));
     BkItem* overflow = reinterpret_cast<BkItem*>(take(bk_b));
     unsigned* cursors = reinterpret_cast<unsigned*>(take(256));
@@ -486,7 +524,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
         HYD_TRY(launch_check("bk_split"));
     }
     HYD_TRY(configure_kernel((const void*)bk_bucket_small_kernel, d, false));
-    bk_bucket_small_kernel<<<(unsigned)(d->sm_count * 4), kBkSmallThreads, kBkSmallSmem, s>>>(
+    bk_bucket_small_kernel<<<(unsigned)(d->sm_count * kBkSmallPerSm), kBkSmallThreads, kBkSmallSmem, s>>>(
         d_inst, d_bk, (unsigned)buckets.size(), cursors + 2, bstart, bcount, keys, vals, overflow, cursors + 4,
         d->d_err);
     HYD_TRY(launch_check("bk_bucket_small"));

@@ -272,9 +272,10 @@ int hyd_cuda_spmv_csr_i32_f64(int64_t nrows, int64_t ncols, const int64_t* row_p
  * x by ncols; y by nrows; row_ptr by nrows + 1 (each instance's row_ptr starts
  * at 0).  Per instance the CSR equals sorting the entries by (row, col) (the
  * packed-key pipeline of bench/coo_csr_build/coo_csr_build.hyd:37-62) and y is
- * its SpMV.  Contract: no duplicate (row, col) in an instance, at most 256
- * entries per row (the workload's cap); a longer row or an out-of-range entry is
- * reported by hyd_cuda_check.  Synchronizes the stream before returning. */
+ * its SpMV; equal (row, col) entries keep their COO order, as the runtime's
+ * stable sort_indices leaves them.  Contract: at most 256 entries per row (the
+ * workload's cap); a longer row or an out-of-range entry is reported by
+ * hyd_cuda_check.  Synchronizes the stream before returning. */
 int hyd_cuda_batched_coo_csr_spmv_f64(int64_t ninst, const int64_t* desc, const int32_t* rows,
                                       const int32_t* cols, const double* vals, const double* x,
                                       int64_t* row_ptr, int32_t* csr_cols, double* csr_vals, double* y,

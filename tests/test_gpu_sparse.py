@@ -101,16 +101,17 @@ def test_spmv_reference_bench(hc, orc, dev, lanes):
 def _check_batch(hc, orc, desc, rows, cols, vals, x, row_ptr, csr_cols, csr_vals, y):
     h_rows, h_cols, h_vals, h_x = (t.cpu().numpy() for t in (rows, cols, vals, x))
     h_rp, h_cc, h_cv, h_y = (t.cpu().numpy() for t in (row_ptr, csr_cols, csr_vals, y))
-    e0 = xr = rp0 = 0
+    e0 = xr = yr = rp0 = 0  # entries, x (by ncols), y (by nrows), row_ptr (by nrows + 1)
     for n, ncols, nnz in desc:
         sl = slice(e0, e0 + nnz)
         rp, ci, cv, yy = orc.coo_to_csr_spmv(n, ncols, h_rows[sl], h_cols[sl], h_vals[sl], h_x[xr:xr + ncols])
         assert np.array_equal(h_rp[rp0:rp0 + n + 1], rp)
         assert np.array_equal(h_cc[sl], ci) and np.array_equal(h_cv[sl], cv)
         bound = orc.spmv_csr(rp, ci.astype(np.int64), np.abs(cv), np.abs(h_x[xr:xr + ncols]))
-        assert np.all(np.abs(h_y[xr:xr + n] - yy) <= 1e-12 * np.maximum(bound, 1e-300))
+        assert np.all(np.abs(h_y[yr:yr + n] - yy) <= 1e-12 * np.maximum(bound, 1e-300))
         e0 += nnz
         xr += ncols
+        yr += n
         rp0 += n + 1
 
 
@@ -161,3 +162,31 @@ def test_bucketed_and_row_atomic_forms_agree(hc, orc, dev, monkeypatch):
     for u, v in zip(a, b):
         assert torch.equal(u, v)
     _check_batch(hc, orc, desc, rows, cols, vals, x, *b)
+
+
+@pytest.mark.parametrize("pipeline", ["bucketed", "rows"])
+def test_batched_pipeline_duplicates_keep_coo_order(hc, orc, dev, pipeline, monkeypatch):
+    """Equal (row, col) entries keep their COO order in the CSR (the runtime's
+    stable sort_indices), in small buckets and in buckets above 2048 entries."""
+    if pipeline == "rows":
+        monkeypatch.setenv("HYD_CUDA_BATCH_PIPELINE", "rows")
+    rng = np.random.default_rng(41)
+    descs, R, Cc, V, X = [], [], [], [], []
+    for n, nnz, ncols, dense in ((50, 400, 7, False), (300, 5000, 300, False), (64, 9000, 40, True),
+                                 (1, 200, 3, False), (4096, 30000, 4096, False)):
+        if dense:  # 64 rows x up to 256 entries: one bucket above the fast kernel's 2048
+            r = np.repeat(np.arange(n), nnz // n)[:nnz]
+            nnz = len(r)
+        else:
+            r = rng.integers(0, n, nnz)
+        c = rng.integers(0, ncols, nnz)  # few columns: many duplicate (row, col)
+        descs.append((n, ncols, nnz))
+        R.append(r); Cc.append(c); V.append(rng.uniform(-1, 1, nnz)); X.append(rng.uniform(-1, 1, ncols))
+    desc = np.array(descs, dtype=np.int64)
+    rows = torch.from_numpy(np.concatenate(R).astype(np.int32)).to(dev)
+    cols = torch.from_numpy(np.concatenate(Cc).astype(np.int32)).to(dev)
+    vals = torch.from_numpy(np.concatenate(V)).to(dev)
+    x = torch.from_numpy(np.concatenate(X)).to(dev)
+    out = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
+    hc.check(hc.device_check())
+    _check_batch(hc, orc, desc, rows, cols, vals, x, *out)
