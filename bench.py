@@ -40,7 +40,13 @@ def parse_args():
     p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="histogram", choices=["histogram"])
+    p.add_argument("--workload", default="histogram", choices=["histogram", "dot", "heat", "batched", "serve"],
+                   help="histogram: the headline line; the others run one configuration of the suite alone "
+                        "(its JSON object on one line; --steps sets its repetitions / heat iterations)")
+    p.add_argument("--variant", type=int, default=-1,
+                   help="heat: run this stencil variant without autotuning (profiling runs)")
+    p.add_argument("--instances", type=int, default=512,
+                   help="batched: number of COO instances (512 is the configuration; fewer for profiling)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-suite", action="store_true",
                    help="skip the other configurations (dot, heat_2d, batched, serving)")
@@ -391,13 +397,22 @@ def _dot_cpu_baseline(O, hx, hy, gpu_value):
             "gpu_rel_err_vs_compensated": abs(gpu_value - ref) / max(1.0, abs(ref))}
 
 
-def suite_heat(hc, torch, peak, iters=1000):
+def suite_heat(hc, torch, peak, iters=1000, variant=-1):
     h = w = 8192
     dev = torch.device("cuda")
     b0 = torch.empty((h, w), dtype=torch.float64, device=dev)
     b1 = torch.empty_like(b0)
     init = torch.empty_like(b0)
     hc.fill_uniform_f64(init, 3, 0.0, 1.0)
+    if variant >= 0:  # a profiling run of one variant: no tuning, no graph
+        side = torch.cuda.current_stream()
+        b0.copy_(init)
+        for _ in range(iters):
+            hc.stencil2d(hc.STENCIL_HEAT, b0, b1, variant=variant)
+            b0, b1 = b1, b0
+        torch.cuda.synchronize()
+        return {"config": "heat_2d 8192^2, %d eager steps of variant %d (%s)" % (iters, variant,
+                                                                               hc.STENCIL_VARIANTS[variant])}
     best, times = hc.autotune_stencil2d(hc.STENCIL_HEAT, h, w, reps=5)
     side = torch.cuda.Stream()
     results = {}
@@ -444,9 +459,9 @@ def suite_heat(hc, torch, peak, iters=1000):
                                  "the 6 per-point operations as exact integer-pipe additions" % emu}}
 
 
-def suite_batched(hc, torch, peak, steps=5):
+def suite_batched(hc, torch, peak, steps=5, instances=512):
     import numpy as np
-    desc, rows, cols, vals, x = hc.synth_coo_batch(512, seed0=4, min_log2=10, max_log2=18, max_row_len=256)
+    desc, rows, cols, vals, x = hc.synth_coo_batch(instances, seed0=4, min_log2=10, max_log2=18, max_row_len=256)
     nnz = int(desc[:, 2].sum())
     n = int(desc[:, 0].sum())
     torch.cuda.synchronize()
@@ -468,8 +483,9 @@ def suite_batched(hc, torch, peak, steps=5):
         p += nr + 1
     alg = 40 * nnz + 32 * n  # COO->CSR read 16 nnz + write 12 nnz + 4(n+1); SpMV 12 nnz + 4(n+1) + 8n + 8n
     gbs = alg / (ms / 1e3) / 1e9
-    res = {"config": "512 instances seeds 4+i, n=2^U(10,18), Zipf(1.5) rows <= 256, int32 rows/cols, f64 vals/x",
-           "instances": 512, "nnz": nnz, "rows": n, "ms": round(ms, 3), "launches": "one persistent pass per stage",
+    res = {"config": "%d instances seeds 4+i, n=2^U(10,18), Zipf(1.5) rows <= 256, int32 rows/cols, f64 vals/x"
+                     % instances,
+           "instances": instances, "nnz": nnz, "rows": n, "ms": round(ms, 3), "launches": "one persistent pass per stage",
            "algorithmic_bytes": alg, "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3),
            "csr_invariants_ok": bool(ok)}
     try:
@@ -684,10 +700,31 @@ def run_reference(args):
     }), flush=True)
 
 
+def run_one(args):
+    """One configuration of the suite alone, on one GPU."""
+    import torch
+    import __graft_entry__ as g
+    hc = g.package()
+    hc.check(hc.lib().hyd_cuda_init())
+    peak = measured_peak()[0]
+    if args.workload == "dot":
+        res = suite_dot(hc, torch, peak, steps=args.steps)
+    elif args.workload == "heat":
+        res = suite_heat(hc, torch, peak, iters=args.steps, variant=args.variant)
+    elif args.workload == "batched":
+        res = suite_batched(hc, torch, peak, steps=args.steps, instances=args.instances)
+    else:
+        res = suite_serve(hc, torch, peak, nreq=args.serve_requests)
+    hc.check(hc.device_check())
+    print(json.dumps({"workload": args.workload, **res}), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "histogram":
+        run_one(args)
     else:
         run_gpu(args)
 

@@ -293,6 +293,17 @@ __device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* 
             acc = fma(val[j], x[c], acc);
         }
     }
+    if (len <= 32) {
+        // the bucketed form's order for short rows: one sum in column order
+        acc = 0.0;
+        for (int i = 0; i < len; ++i) {
+            const long long k = __shfl_sync(0xffffffffu, key[0], i);
+            const double v = __shfl_sync(0xffffffffu, val[0], i);
+            acc = fma(v, x[(int)(k >> 32)], acc);
+        }
+        if (lane == 0) *yrow = acc;
+        return;
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) *yrow = acc;

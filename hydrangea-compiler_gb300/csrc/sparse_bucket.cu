@@ -110,7 +110,7 @@ __global__ void bk_widen_kernel(const unsigned* __restrict__ c, long long* __res
 
 // Stage 3.
 constexpr int kSplitPer = kTileEntries / kBkThreads;  // 16 entries per thread
-__global__ void __launch_bounds__(kBkThreads) bk_split_kernel(const BkInst* __restrict__ inst,
+__global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* __restrict__ inst,
                                                               const BkItem* __restrict__ items, unsigned nitems,
                                                               unsigned* cursor, const long long* __restrict__ bstart,
                                                               unsigned* __restrict__ bfill,
@@ -332,9 +332,26 @@ __global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_smal
             if (r < nr) I.row_ptr[r0 + r] = e0 + dbase[r];
             else if (r0 + nr == I.nrows) I.row_ptr[I.nrows] = I.nnz;
         }
+        // SpMV.  Rows of at most 32 entries: one lane per row, summed in column
+        // order (warps 0-1 cover the bucket's 64 rows).  Longer rows: a warp,
+        // lane i summing positions i, i+32, ..., then a fixed xor tree.  (On
+        // GB300 every FP64 warp instruction holds the FP64 pipe for ~64 cycles,
+        // so a tree per short row would cost more than the row itself.)
+        auto row_end = [&](int r) { return r + 1 < nr ? (int)dbase[r + 1] : E; };
+        if (warp < kBkRows / 32) {
+            const int r = warp * 32 + lane;
+            if (r < nr) {
+                const int a = (int)dbase[r], bb = row_end(r);
+                if (bb - a <= 32) {
+                    double acc = 0.0;
+                    for (int p = a; p < bb; ++p) acc = fma(vals_in[s0 + iin[p]], I.x[kin[p] & cmask], acc);
+                    I.y[r0 + r] = acc;
+                }
+            }
+        }
         for (int r = warp; r < nr; r += kBkSmallWarps) {
-            const int a = (int)dbase[r], b = r + 1 < kBkRows ? (int)dbase[r + 1] : E;
-            const int bb = r + 1 < nr ? b : E;
+            const int a = (int)dbase[r], bb = row_end(r);
+            if (bb - a <= 32) continue;  // warp-uniform
             if (bb - a > 256) bad = true;  // a row above 256 entries: outside the contract
             double acc = 0.0;
             for (int p = a + lane; p < bb; p += 32)
@@ -421,7 +438,18 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
             if (r < nr) I.row_ptr[r0 + r] = e0 + rstart[r];
             else if (r0 + nr == I.nrows) I.row_ptr[I.nrows] = I.nnz;
         }
+        // SpMV as in the fast kernel: short rows one lane each, long rows a warp
+        if (warp < kBkRows / 32) {
+            const int r = warp * 32 + lane;
+            if (r < nr && rstart[r + 1] - rstart[r] <= 32) {
+                double acc = 0.0;
+                for (int p = rstart[r]; p < rstart[r + 1]; ++p)
+                    acc = fma(vals_in[s0 + idx[p]], I.x[key[p] & 0xFFFFFFu], acc);
+                I.y[r0 + r] = acc;
+            }
+        }
         for (int r = warp; r < nr; r += kBkThreads / 32) {
+            if (rstart[r + 1] - rstart[r] <= 32) continue;  // warp-uniform
             double acc = 0.0;
             for (int p = rstart[r] + lane; p < rstart[r + 1]; p += 32)
                 acc = fma(vals_in[s0 + idx[p]], I.x[key[p] & 0xFFFFFFu], acc);
