@@ -114,8 +114,7 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
                                                               const BkItem* __restrict__ items, unsigned nitems,
                                                               unsigned* cursor, const long long* __restrict__ bstart,
                                                               unsigned* __restrict__ bfill,
-                                                              uint2* __restrict__ keys_out,
-                                                              double* __restrict__ vals_out) {
+                                                              uint4* __restrict__ rec_out) {
     __shared__ unsigned hist[kMaxSmemBuckets];
     __shared__ unsigned gbase[kMaxSmemBuckets];  // batch-wide slots (< 2^32, checked on the host)
     unsigned it;
@@ -145,9 +144,21 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
         }
         __syncthreads();
         if (smem) {
-            for (int b = threadIdx.x; b < I.nbuckets; b += kBkThreads) {
-                const unsigned c = hist[b];
-                gbase[b] = c ? (unsigned)(bstart[I.bucket_base + b] + atomicAdd(&bfill[I.bucket_base + b], c)) : 0u;
+            // reserve this tile's run in every non-empty bucket; the atomics of
+            // one thread are independent, so they are all issued before any
+            // result is used (one memory round trip instead of eight)
+            constexpr int kPerThread = kMaxSmemBuckets / kBkThreads;
+            unsigned got[kPerThread];
+#pragma unroll
+            for (int q = 0; q < kPerThread; ++q) {
+                const int b = threadIdx.x + q * kBkThreads;
+                const unsigned c = b < I.nbuckets ? hist[b] : 0u;
+                got[q] = c ? atomicAdd(&bfill[I.bucket_base + b], c) : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < kPerThread; ++q) {
+                const int b = threadIdx.x + q * kBkThreads;
+                if (b < I.nbuckets && hist[b]) gbase[b] = (unsigned)(bstart[I.bucket_base + b] + got[q]);
             }
         }
         __syncthreads();
@@ -158,9 +169,10 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
             const long long pos = smem ? (long long)gbase[bucket[j]] + rank[j]
                                        : bstart[I.bucket_base + bucket[j]] +
                                              atomicAdd(&bfill[I.bucket_base + bucket[j]], 1u);
-            // the key and the entry's COO position (orders equal (row, col) keys)
-            keys_out[pos] = make_uint2(key[j], (unsigned)k);
-            vals_out[pos] = I.vals[k];
+            // one 16-byte record: the key, the entry's COO position (orders
+            // equal (row, col) keys) and the value
+            const double v = I.vals[k];
+            rec_out[pos] = make_uint4(key[j], (unsigned)k, (unsigned)__double2loint(v), (unsigned)__double2hiint(v));
         }
         __syncthreads();
     }
@@ -178,9 +190,11 @@ constexpr size_t kBkSmallSmem = (size_t)kBkSmallCap * 12 + (size_t)kBkSmallWarps
 // sort_indices).  The split's order inside a bucket is arbitrary, so after the
 // sort every run of equal keys is put in COO-position order (insertion sort
 // by the thread that owns the run's first slot; duplicates are rare).
+__device__ __forceinline__ double bk_rec_val(const uint4& r) { return __hiloint2double((int)r.w, (int)r.z); }
+
 template <class IdxT>
 __device__ __forceinline__ void bk_order_equal_keys(const unsigned* key, IdxT* pos, int E,
-                                                    const uint2* __restrict__ rec) {
+                                                    const uint4* __restrict__ rec) {
     for (int p = threadIdx.x; p + 1 < E; p += blockDim.x) {
         if (key[p + 1] != key[p] || (p > 0 && key[p - 1] == key[p])) continue;
         int q = p + 2;
@@ -209,8 +223,8 @@ __device__ __forceinline__ void bk_order_equal_keys(const unsigned* key, IdxT* p
 constexpr int kBkSmallPerSm = 6;  // resident CTAs per SM
 __global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_small_kernel(
     const BkInst* __restrict__ inst, const BkItem* __restrict__ items, unsigned nitems, unsigned* cursor,
-    const long long* __restrict__ bstart, const unsigned* __restrict__ bcount, const uint2* __restrict__ keys_in,
-    const double* __restrict__ vals_in, BkItem* __restrict__ overflow, unsigned* overflow_count, unsigned* err) {
+    const long long* __restrict__ bstart, const unsigned* __restrict__ bcount, const uint4* __restrict__ rec_in,
+    BkItem* __restrict__ overflow, unsigned* overflow_count, unsigned* err) {
     extern __shared__ __align__(16) unsigned char bks_smem[];
     unsigned* kbuf0 = reinterpret_cast<unsigned*>(bks_smem);
     unsigned* kbuf1 = kbuf0 + kBkSmallCap;
@@ -241,7 +255,7 @@ __global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_smal
         // key = row_in_bucket << cbits | col: 6 + cbits bits, 8 per pass
         const int passes = (kBkShift + cbits + 7) / 8;
         for (int i = threadIdx.x; i < E; i += kBkSmallThreads) {
-            const unsigned k = keys_in[s0 + i].x;
+            const unsigned k = rec_in[s0 + i].x;
             kbuf0[i] = ((k >> 24) << cbits) | (k & 0xFFFFFFu);
             ibuf0[i] = (unsigned short)i;
         }
@@ -322,11 +336,11 @@ __global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_smal
             const int rc = p == E ? kBkRows : (int)(kin[p] >> cbits);
             for (int r = rp + 1; r <= rc && r < kBkRows; ++r) dbase[r] = (unsigned)p;
         }
-        bk_order_equal_keys(kin, iin, E, keys_in + s0);
+        bk_order_equal_keys(kin, iin, E, rec_in + s0);
         __syncthreads();
         for (int p = threadIdx.x; p < E; p += kBkSmallThreads) {
             I.csr_cols[e0 + p] = (int)(kin[p] & cmask);
-            I.csr_vals[e0 + p] = vals_in[s0 + iin[p]];
+            I.csr_vals[e0 + p] = bk_rec_val(rec_in[s0 + iin[p]]);
         }
         for (int r = threadIdx.x; r <= nr; r += kBkSmallThreads) {
             if (r < nr) I.row_ptr[r0 + r] = e0 + dbase[r];
@@ -344,7 +358,7 @@ __global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_smal
                 const int a = (int)dbase[r], bb = row_end(r);
                 if (bb - a <= 32) {
                     double acc = 0.0;
-                    for (int p = a; p < bb; ++p) acc = fma(vals_in[s0 + iin[p]], I.x[kin[p] & cmask], acc);
+                    for (int p = a; p < bb; ++p) acc = fma(bk_rec_val(rec_in[s0 + iin[p]]), I.x[kin[p] & cmask], acc);
                     I.y[r0 + r] = acc;
                 }
             }
@@ -355,7 +369,7 @@ __global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_smal
             if (bb - a > 256) bad = true;  // a row above 256 entries: outside the contract
             double acc = 0.0;
             for (int p = a + lane; p < bb; p += 32)
-                acc = fma(vals_in[s0 + iin[p]], I.x[kin[p] & cmask], acc);
+                acc = fma(bk_rec_val(rec_in[s0 + iin[p]]), I.x[kin[p] & cmask], acc);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) I.y[r0 + r] = acc;
@@ -375,8 +389,7 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
                                                                const unsigned* nitems_dev, unsigned* cursor,
                                                                const long long* __restrict__ bstart,
                                                                const unsigned* __restrict__ bcount,
-                                                               const uint2* __restrict__ keys_in,
-                                                               const double* __restrict__ vals_in, unsigned* err) {
+                                                               const uint4* __restrict__ rec_in, unsigned* err) {
     extern __shared__ __align__(16) unsigned char bk_smem[];
     unsigned* key = reinterpret_cast<unsigned*>(bk_smem);
     unsigned short* idx = reinterpret_cast<unsigned short*>(bk_smem + (size_t)kBkCap * 4);
@@ -401,7 +414,7 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
         int P = 1;
         while (P < E) P <<= 1;
         for (int i = threadIdx.x; i < P; i += kBkThreads) {
-            key[i] = i < E ? keys_in[s0 + i].x : 0xFFFFFFFFu;
+            key[i] = i < E ? rec_in[s0 + i].x : 0xFFFFFFFFu;
             idx[i] = (unsigned short)i;
         }
         __syncthreads();
@@ -428,11 +441,11 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
             const int rc = p == E ? nr : (int)(key[p] >> 24);
             for (int r = rp + 1; r <= rc && r <= nr; ++r) rstart[r] = p;
         }
-        bk_order_equal_keys(key, idx, E, keys_in + s0);  // the bitonic network is not stable
+        bk_order_equal_keys(key, idx, E, rec_in + s0);  // the bitonic network is not stable
         __syncthreads();
         for (int p = threadIdx.x; p < E; p += kBkThreads) {
             I.csr_cols[e0 + p] = (int)(key[p] & 0xFFFFFFu);
-            I.csr_vals[e0 + p] = vals_in[s0 + idx[p]];
+            I.csr_vals[e0 + p] = bk_rec_val(rec_in[s0 + idx[p]]);
         }
         for (int r = threadIdx.x; r <= nr; r += kBkThreads) {
             if (r < nr) I.row_ptr[r0 + r] = e0 + rstart[r];
@@ -444,7 +457,7 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
             if (r < nr && rstart[r + 1] - rstart[r] <= 32) {
                 double acc = 0.0;
                 for (int p = rstart[r]; p < rstart[r + 1]; ++p)
-                    acc = fma(vals_in[s0 + idx[p]], I.x[key[p] & 0xFFFFFFu], acc);
+                    acc = fma(bk_rec_val(rec_in[s0 + idx[p]]), I.x[key[p] & 0xFFFFFFu], acc);
                 I.y[r0 + r] = acc;
             }
         }
@@ -452,7 +465,7 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
             if (rstart[r + 1] - rstart[r] <= 32) continue;  // warp-uniform
             double acc = 0.0;
             for (int p = rstart[r] + lane; p < rstart[r + 1]; p += 32)
-                acc = fma(vals_in[s0 + idx[p]], I.x[key[p] & 0xFFFFFFu], acc);
+                acc = fma(bk_rec_val(rec_in[s0 + idx[p]]), I.x[key[p] & 0xFFFFFFu], acc);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) I.y[r0 + r] = acc;
@@ -517,8 +530,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     unsigned* bfill = reinterpret_cast<unsigned*>(take(cnt_b));
     long long* wide = reinterpret_cast<long long*>(take(wide_b));
     long long* bstart = reinterpret_cast<long long*>(take(wide_b));
-    uint2* keys = reinterpret_cast<uint2*>(take(vals_b));  // (key, COO position) per entry
-    double* vals = reinterpret_cast<double*>(take(vals_b));
+    uint4* recs = reinterpret_cast<uint4*>(take(2 * vals_b));  // (key, COO position, value) per entry
     BkItem* overflow = reinterpret_cast<BkItem*>(take(bk_b));
     unsigned* cursors = reinterpret_cast<unsigned*>(take(256));
     const size_t table = inst_b + tiles_b + bk_b;
@@ -548,17 +560,16 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     HYD_TRY(scan_i64_launch(wide, bstart, nb_total, 0, false, false, s));
     if (!tiles.empty()) {
         bk_split_kernel<<<grid, kBkThreads, 0, s>>>(d_inst, d_tiles, (unsigned)tiles.size(), cursors + 1, bstart,
-                                                    bfill, keys, vals);
+                                                    bfill, recs);
         HYD_TRY(launch_check("bk_split"));
     }
     HYD_TRY(configure_kernel((const void*)bk_bucket_small_kernel, d, false));
     bk_bucket_small_kernel<<<(unsigned)(d->sm_count * kBkSmallPerSm), kBkSmallThreads, kBkSmallSmem, s>>>(
-        d_inst, d_bk, (unsigned)buckets.size(), cursors + 2, bstart, bcount, keys, vals, overflow, cursors + 4,
-        d->d_err);
+        d_inst, d_bk, (unsigned)buckets.size(), cursors + 2, bstart, bcount, recs, overflow, cursors + 4, d->d_err);
     HYD_TRY(launch_check("bk_bucket_small"));
     HYD_TRY(configure_kernel((const void*)bk_bucket_kernel, d, false));
     bk_bucket_kernel<<<grid, kBkThreads, kBkSmem, s>>>(d_inst, overflow, cursors + 4, cursors + 3, bstart, bcount,
-                                                       keys, vals, d->d_err);
+                                                       recs, d->d_err);
     HYD_TRY(launch_check("bk_bucket_large"));
     if (!async_tables) HYD_CUDA_TRY(cudaStreamSynchronize(s));
     return HYD_CUDA_OK;
