@@ -591,7 +591,7 @@ def suite_serve(hc, torch, peak, nreq=100_000, lam=20_000.0):
     pool, keep = _serve_pool(hc, torch)
     reqs, arr = _trace(pool, nreq, lam, 5)
     budget = 16 << 30
-    srv = hc.Server(budget_bytes=budget, streams=4, max_batch=32)
+    srv = hc.Server(budget_bytes=budget, streams=8, max_batch=128)
     try:
         lat_s, st_s, el_s = srv.trace(reqs, arr)
         stats = srv.stats()
@@ -605,7 +605,7 @@ def suite_serve(hc, torch, peak, nreq=100_000, lam=20_000.0):
     # saturation: everything arrives at once
     nsat = min(nreq, 20_000)
     sreqs, sarr = _trace(pool, nsat, 0, 6)
-    srv = hc.Server(budget_bytes=budget, streams=4, max_batch=32)
+    srv = hc.Server(budget_bytes=budget, streams=8, max_batch=128)
     try:
         l1, s1, e1 = srv.trace(sreqs, sarr)
     finally:

@@ -27,7 +27,7 @@ namespace hyd {
 // The fallback lives behind a call so that the compiler cannot if-convert it
 // into an unconditional FP64 add on every lane: warps whose operands are all
 // on the fast path branch over it and issue nothing on the FP64 pipe.
-__device__ __noinline__ double dadd_fallback(double x, double y) { return __dadd_rn(x, y); }
+static __device__ __noinline__ double dadd_fallback(double x, double y) { return __dadd_rn(x, y); }
 
 __device__ __forceinline__ double dadd_pos(double x, double y) {
     const unsigned long long X = (unsigned long long)__double_as_longlong(x);

@@ -136,8 +136,9 @@ __global__ void __launch_bounds__(kMixThreads, 2)
             if (sh_last && threadIdx.x < 32) {
                 __threadfence();
                 double s = 0.0;
-                const volatile double* p = reinterpret_cast<const volatile double*>(scratch) + R.scratch;
-                for (long long t = threadIdx.x; t < R.nitems; t += 32) s += p[t];
+                // L2 loads (the partials were fenced by their writers), all in flight
+                const double* p = reinterpret_cast<const double*>(scratch) + R.scratch;
+                for (long long t = threadIdx.x; t < R.nitems; t += 32) s += __ldcg(p + t);
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
                 if (threadIdx.x == 0) *static_cast<double*>(R.out) = s;
@@ -157,14 +158,31 @@ __global__ void __launch_bounds__(kMixThreads, 2)
             const long long base = tile * kHistTile;
             const long long len = R.n - base < kHistTile ? R.n - base : kHistTile;
             bool bad = false;
-            for (long long i = threadIdx.x; i < len; i += kMixThreads) {
-                const long long x = data[base + i];
+            auto add1 = [&](long long x) {
                 const long long b = pow2 ? ((x >= 0 || (x & (bins - 1)) == 0) ? (x & (bins - 1)) : -1) : x % bins;
                 if ((unsigned long long)b < (unsigned long long)bins)
                     limb_add32(lo_l, hi_l, (unsigned)b, (unsigned long long)x * (unsigned long long)x);
                 else
                     bad = true;
+            };
+            long long tail = 0;
+            if ((reinterpret_cast<uintptr_t>(data + base) & 31) == 0) {  // 32-byte vectors, two in flight
+                const long long nv = len >> 2;
+                long long v = threadIdx.x;
+                for (; v + kMixThreads < nv; v += 2 * kMixThreads) {
+                    const u64x4 q0 = ldg_stream_u64x4(reinterpret_cast<const unsigned long long*>(data + base) + 4 * v);
+                    const u64x4 q1 = ldg_stream_u64x4(reinterpret_cast<const unsigned long long*>(data + base) +
+                                                      4 * (v + kMixThreads));
+                    add1((long long)q0.x); add1((long long)q0.y); add1((long long)q0.z); add1((long long)q0.w);
+                    add1((long long)q1.x); add1((long long)q1.y); add1((long long)q1.z); add1((long long)q1.w);
+                }
+                for (; v < nv; v += kMixThreads) {
+                    const u64x4 q = ldg_stream_u64x4(reinterpret_cast<const unsigned long long*>(data + base) + 4 * v);
+                    add1((long long)q.x); add1((long long)q.y); add1((long long)q.z); add1((long long)q.w);
+                }
+                tail = nv * 4;
             }
+            for (long long i = tail + threadIdx.x; i < len; i += kMixThreads) add1(data[base + i]);
             if (bad) status[R.index] = HYD_CUDA_ERR_BOUNDS;
             __syncthreads();
             unsigned long long* part = scratch + R.scratch + tile * (long long)bins;
@@ -182,12 +200,20 @@ __global__ void __launch_bounds__(kMixThreads, 2)
             __syncthreads();
             if (sh_last) {
                 __threadfence();
-                const volatile unsigned long long* p = scratch + R.scratch;
+                // L2 loads (the partials were fenced by their writers), four in flight
+                const unsigned long long* p = scratch + R.scratch;
                 unsigned long long* out = static_cast<unsigned long long*>(R.out);
                 for (int b = threadIdx.x; b < bins; b += kMixThreads) {
-                    unsigned long long s = 0;
-                    for (long long t = 0; t < R.nitems; ++t) s += p[t * bins + b];
-                    out[b] = s;
+                    unsigned long long s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                    long long t = 0;
+                    for (; t + 3 < R.nitems; t += 4) {
+                        s0 += __ldcg(p + t * bins + b);
+                        s1 += __ldcg(p + (t + 1) * bins + b);
+                        s2 += __ldcg(p + (t + 2) * bins + b);
+                        s3 += __ldcg(p + (t + 3) * bins + b);
+                    }
+                    for (; t < R.nitems; ++t) s0 += __ldcg(p + t * bins + b);
+                    out[b] = (s0 + s1) + (s2 + s3);  // integer sums: order-free
                 }
             }
             __syncthreads();  // shared bins are reused by the next item
