@@ -86,8 +86,8 @@ __global__ void __launch_bounds__(kBkThreads) bk_count_kernel(const BkInst* __re
         const long long t0 = (long long)w.tile * kTileEntries;
         const long long t1 = t0 + kTileEntries < I.nnz ? t0 + kTileEntries : I.nnz;
         for (long long k = t0 + threadIdx.x; k < t1; k += kBkThreads) {
-            const int r = I.rows[k], c = I.cols[k];
-            if (r < 0 || r >= I.nrows || c < 0 || c >= I.ncols) {
+            const int r = I.rows[k];  // columns are checked by the split, which reads them anyway
+            if (r < 0 || r >= I.nrows) {
                 bad = true;
                 continue;
             }
@@ -114,10 +114,11 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
                                                               const BkItem* __restrict__ items, unsigned nitems,
                                                               unsigned* cursor, const long long* __restrict__ bstart,
                                                               unsigned* __restrict__ bfill,
-                                                              uint4* __restrict__ rec_out) {
+                                                              uint4* __restrict__ rec_out, unsigned* err) {
     __shared__ unsigned hist[kMaxSmemBuckets];
     __shared__ unsigned gbase[kMaxSmemBuckets];  // batch-wide slots (< 2^32, checked on the host)
     unsigned it;
+    bool bad = false;
     while (bk_next(cursor, nitems, it)) {
         const BkItem w = items[it];
         const BkInst I = inst[w.inst];
@@ -135,7 +136,8 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
             bucket[j] = -1;
             if (k < t1) {
                 const int r = I.rows[k], c = I.cols[k];
-                if (r >= 0 && r < I.nrows && c >= 0 && c < I.ncols) {  // invalid ones were reported by stage 1
+                if (c < 0 || c >= I.ncols) bad = true;                 // (rows were checked by the count)
+                if (r >= 0 && r < I.nrows && c >= 0 && c < I.ncols) {
                     bucket[j] = r >> kBkShift;
                     key[j] = ((unsigned)(r & (kBkRows - 1)) << 24) | (unsigned)c;
                     if (smem) rank[j] = atomicAdd(&hist[bucket[j]], 1u);
@@ -176,6 +178,7 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
         }
         __syncthreads();
     }
+    if (bad) raise_error(err, ERRBIT_BOUNDS);
 }
 
 // ---- stage 4 ------------------------------------------------------------------
@@ -560,7 +563,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     HYD_TRY(scan_i64_launch(wide, bstart, nb_total, 0, false, false, s));
     if (!tiles.empty()) {
         bk_split_kernel<<<grid, kBkThreads, 0, s>>>(d_inst, d_tiles, (unsigned)tiles.size(), cursors + 1, bstart,
-                                                    bfill, recs);
+                                                    bfill, recs, d->d_err);
         HYD_TRY(launch_check("bk_split"));
     }
     HYD_TRY(configure_kernel((const void*)bk_bucket_small_kernel, d, false));

@@ -190,3 +190,18 @@ def test_batched_pipeline_duplicates_keep_coo_order(hc, orc, dev, pipeline, monk
     out = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
     hc.check(hc.device_check())
     _check_batch(hc, orc, desc, rows, cols, vals, x, *out)
+
+
+@pytest.mark.parametrize("pipeline", ["bucketed", "rows"])
+@pytest.mark.parametrize("bad", ["row", "col"])
+def test_batched_out_of_range_entry_reported(hc, orc, dev, pipeline, bad, monkeypatch):
+    if pipeline == "rows":
+        monkeypatch.setenv("HYD_CUDA_BATCH_PIPELINE", "rows")
+    desc, rows, cols, vals, x = hc.synth_coo_batch(3, seed0=77, min_log2=8, max_log2=10)
+    if bad == "row":
+        rows[5] = int(desc[0, 0])       # one past the first instance's last row
+    else:
+        cols[7] = -1
+    hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
+    assert hc.device_check() == hc.ERR_BOUNDS
+    assert hc.device_check() == hc.OK
