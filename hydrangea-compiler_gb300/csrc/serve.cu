@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "batch.cuh"
+#include "fp64_emu.cuh"
 #include "hyd_common.cuh"
 
 namespace hyd {
@@ -40,7 +41,8 @@ namespace hyd {
 constexpr int kMixThreads = 512;
 constexpr long long kDotTile = 1LL << 16;
 constexpr long long kHistTile = 1LL << 18;
-constexpr int kLapTH = 16, kLapTW = 128;
+constexpr int kLapTH = 64, kLapTW = 128;
+static_assert(kLapTH * kLapTW % kMixThreads == 0 && kMixThreads % kLapTW == 0, "Laplacian tile vs threads");
 constexpr int kMixMaxBins = 8192;  // histogram requests served up to this many bins
 constexpr size_t kMixSmem = 64 * 1024;
 
@@ -57,8 +59,9 @@ struct MixReq {
 };
 
 __device__ __forceinline__ double lap_body(double a, double b, double c, double d, double e) {
-    // a + b + c + d + (e * -4.0), evaluated as the C backend does (4e exact)
-    const double t3 = __dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d);
+    // a + b + c + d + (e * -4.0), evaluated as the C backend does (4e exact);
+    // the first two additions on the integer pipe (exact, FP64 fallback)
+    const double t3 = __dadd_rn(dadd_pos(dadd_pos(a, b), c), d);
     return __fma_rn(e, -4.0, t3);
 }
 
@@ -218,17 +221,30 @@ __global__ void __launch_bounds__(kMixThreads, 2)
             }
             __syncthreads();  // shared bins are reused by the next item
         } else {  // HYD_REQ_LAPLACIAN, one clamp step
+            // a thread sweeps kRowsPer rows of one column, carrying the rows
+            // above and at the point in registers: three loads per point
             const double* in = static_cast<const double*>(R.a);
             double* out = static_cast<double*>(R.out);
             const long long h = R.n, w = R.m;
             const long long ntj = (w + kLapTW - 1) / kLapTW;
             const long long i0 = (tile / ntj) * kLapTH, j0 = (tile % ntj) * kLapTW;
-            for (int p = threadIdx.x; p < kLapTH * kLapTW; p += kMixThreads) {
-                const long long i = i0 + p / kLapTW, j = j0 + p % kLapTW;
-                if (i >= h || j >= w) continue;
-                const long long im = i > 0 ? i - 1 : 0, ip = i + 1 < h ? i + 1 : h - 1;
+            constexpr int kRowsPer = kLapTH * kLapTW / kMixThreads;
+            const long long j = j0 + (threadIdx.x % kLapTW);
+            const long long ib = i0 + (threadIdx.x / kLapTW) * kRowsPer;
+            if (j < w && ib < h) {
                 const long long jm = j > 0 ? j - 1 : 0, jp = j + 1 < w ? j + 1 : w - 1;
-                out[i * w + j] = lap_body(in[im * w + j], in[ip * w + j], in[i * w + jm], in[i * w + jp], in[i * w + j]);
+                double up = in[(ib > 0 ? ib - 1 : 0) * w + j];
+                double mid = in[ib * w + j];
+#pragma unroll
+                for (int k = 0; k < kRowsPer; ++k) {
+                    const long long i = ib + k;
+                    if (i >= h) break;
+                    const double dn = in[(i + 1 < h ? i + 1 : h - 1) * w + j];
+                    const double* row = in + i * w;
+                    out[i * w + j] = lap_body(up, dn, row[jm], row[jp], mid);
+                    up = mid;
+                    mid = dn;
+                }
             }
         }
     }
