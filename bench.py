@@ -40,7 +40,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="histogram", choices=["histogram", "dot", "heat", "batched", "serve"],
+    p.add_argument("--workload", default="histogram",
+                   choices=["histogram", "dot", "heat", "jacobi1d", "gray_scott", "batched", "serve"],
                    help="histogram: the headline line; the others run one configuration of the suite alone "
                         "(its JSON object on one line; --steps sets its repetitions / heat iterations)")
     p.add_argument("--variant", type=int, default=-1,
@@ -459,6 +460,58 @@ def suite_heat(hc, torch, peak, iters=1000, variant=-1):
                                  "the 6 per-point operations as exact integer-pipe additions" % emu}}
 
 
+def suite_jacobi1d(hc, torch, peak, iters=100):
+    """jacobi_1d (examples/jacobi_1d.hyd) over n = 2^25 float64, a captured graph."""
+    n = 1 << 25
+    dev = torch.device("cuda")
+    b0 = torch.empty(n, dtype=torch.float64, device=dev)
+    b1 = torch.empty_like(b0)
+    hc.fill_uniform_f64(b0, 7, 0.0, 1.0)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        hc.iterate_jacobi1d(b0, b1, iters, stream=side)  # builds the graph
+        side.synchronize()
+        e0, e1 = _events(torch, side)
+        e0.record(side)
+        hc.iterate_jacobi1d(b0, b1, iters, stream=side)
+        e1.record(side)
+    side.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    gbs = 16 * n / (ms / 1e3) / 1e9
+    return {"config": "jacobi_1d (a[i-1] + a[i] + a[i+1]) / 3.0 clamp, n=2^25 f64 U[0,1) seed 7, %d steps, CUDA graph"
+                      % iters, "ms_per_step": round(ms, 4), "GB_s": round(gbs, 1),
+            "frac_of_hbm_peak": round(gbs / peak, 3),
+            "note": "one IEEE division per point on GB300's FP64 unit (1.9 DFMA/clk/SM) bounds it"}
+
+
+def suite_gray_scott(hc, torch, peak, steps=5000):
+    """Gray-Scott (demo/gray_scott/gray_scott.hyd): the demo's 256^2 x 5000 steps
+    (launch-bound: a captured graph) and a 4096^2 grid (throughput)."""
+    import numpy as np
+    dev = torch.device("cuda")
+    out = {}
+    for (h, w, k) in ((256, 256, steps), (4096, 4096, max(steps // 50, 4))):
+        bufs = [torch.empty((h, w), dtype=torch.float64, device=dev) for _ in range(4)]
+        bufs[0].fill_(1.0)
+        hc.fill_uniform_f64(bufs[1], 8, 0.0, 0.5)
+        side = torch.cuda.Stream()
+        with torch.cuda.stream(side):
+            hc.iterate_gray_scott(bufs[0], bufs[1], bufs[2], bufs[3], k, stream=side)  # builds the graph
+            side.synchronize()
+            e0, e1 = _events(torch, side)
+            e0.record(side)
+            hc.iterate_gray_scott(bufs[0], bufs[1], bufs[2], bufs[3], k, stream=side)
+            e1.record(side)
+        side.synchronize()
+        ms = e0.elapsed_time(e1)
+        gbs = 32 * h * w * k / (ms / 1e3) / 1e9
+        out["%dx%d" % (h, w)] = {"steps": k, "total_ms": round(ms, 3), "us_per_step": round(1e3 * ms / k, 2),
+                                 "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3)}
+        del bufs
+    out["config"] = "gray_scott U,V periodic, du 0.21 dv 0.105 feed 0.0545 kill 0.062 dt 1, CUDA graph"
+    return out
+
+
 def suite_batched(hc, torch, peak, steps=5, instances=512):
     import numpy as np
     desc, rows, cols, vals, x = hc.synth_coo_batch(instances, seed0=4, min_log2=10, max_log2=18, max_row_len=256)
@@ -622,7 +675,8 @@ def suite_serve(hc, torch, peak, nreq=100_000, lam=20_000.0):
 
 def run_suite(hc, torch, args, peak):
     out = {}
-    for name, fn in (("dot", suite_dot), ("heat_2d", suite_heat), ("batched_coo_csr_spmv", suite_batched),
+    for name, fn in (("dot", suite_dot), ("heat_2d", suite_heat), ("jacobi_1d", suite_jacobi1d),
+                     ("gray_scott", suite_gray_scott), ("batched_coo_csr_spmv", suite_batched),
                      ("serving", lambda a, b, c: suite_serve(a, b, c, nreq=args.serve_requests))):
         t = time.perf_counter()
         try:
@@ -711,6 +765,10 @@ def run_one(args):
         res = suite_dot(hc, torch, peak, steps=args.steps)
     elif args.workload == "heat":
         res = suite_heat(hc, torch, peak, iters=args.steps, variant=args.variant)
+    elif args.workload == "jacobi1d":
+        res = suite_jacobi1d(hc, torch, peak, iters=args.steps)
+    elif args.workload == "gray_scott":
+        res = suite_gray_scott(hc, torch, peak, steps=args.steps)
     elif args.workload == "batched":
         res = suite_batched(hc, torch, peak, steps=args.steps, instances=args.instances)
     else:

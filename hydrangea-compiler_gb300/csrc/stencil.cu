@@ -434,10 +434,17 @@ extern "C" int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* bu
     return hyd_cuda_iterate_stencil2d_f64_variant(kind, buf0, buf1, h, w, iters, -1, final_buf, stream);
 }
 
+namespace hyd {
+void release_more_graphs();  // stencil_more.cu
+}
+
 extern "C" void hyd_cuda_stencil_release_graphs(void) {
-    std::lock_guard<std::mutex> lock(g_graph_mu);
-    for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
-    g_graphs.clear();
+    {
+        std::lock_guard<std::mutex> lock(g_graph_mu);
+        for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
+        g_graphs.clear();
+    }
+    release_more_graphs();
 }
 
 // ---------------------------------------------------------------- self-test

@@ -88,6 +88,11 @@ SIGNATURES = {
     "hyd_cuda_array_alloc": (_p, [None, C.c_size_t]),
     "hyd_export_weighted_histogram": (_p, [_p, _i64]),
     "hyd_export_dot": (_d, [_p, _p]),
+    "hyd_export_gray_scott": (_p, []),
+    "hyd_cuda_jacobi1d_f64": (_i, [_p, _p, _i64, _p]),
+    "hyd_cuda_iterate_jacobi1d_f64": (_i, [_p, _p, _i64, _i64, C.POINTER(C.c_int), _p]),
+    "hyd_cuda_gray_scott_step_f64": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _p]),
+    "hyd_cuda_iterate_gray_scott_f64": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _i64, C.POINTER(C.c_int), _p]),
 }
 
 
@@ -256,6 +261,43 @@ def iterate_stencil2d(kind, buf0, buf1, iters, stream=None, variant=-1):
     call("hyd_cuda_iterate_stencil2d_f64_variant", kind, ptr(buf0), ptr(buf1), h, w, iters, variant,
          C.byref(fb), stream_handle(stream))
     return buf0 if fb.value == 0 else buf1
+
+
+class GrayScott(C.Structure):
+    """hyd_gray_scott_t; defaults are demo/gray_scott/gray_scott.hyd:19-25."""
+    _fields_ = [("du", C.c_double), ("dv", C.c_double), ("feed", C.c_double), ("kill", C.c_double),
+                ("dt", C.c_double)]
+
+    def __init__(self, du=0.21, dv=0.105, feed=0.0545, kill=0.0620, dt=1.0):
+        super().__init__(du, dv, feed, kill, dt)
+
+
+def jacobi1d(src, dst, stream=None):
+    call("hyd_cuda_jacobi1d_f64", ptr(src), ptr(dst), src.numel(), stream_handle(stream))
+
+
+def iterate_jacobi1d(buf0, buf1, iters, stream=None):
+    """Runs iters steps; returns the buffer holding the result."""
+    which = C.c_int(0)
+    call("hyd_cuda_iterate_jacobi1d_f64", ptr(buf0), ptr(buf1), buf0.numel(), iters, C.byref(which),
+         stream_handle(stream))
+    return buf1 if which.value else buf0
+
+
+def gray_scott_step(u, v, u_out, v_out, params=None, stream=None):
+    h, w = u.shape
+    p = C.byref(params) if params is not None else None
+    call("hyd_cuda_gray_scott_step_f64", ptr(u), ptr(v), ptr(u_out), ptr(v_out), h, w, p, stream_handle(stream))
+
+
+def iterate_gray_scott(u0, v0, u1, v1, steps, params=None, stream=None):
+    """Runs steps steps; returns the (u, v) buffers holding the result."""
+    h, w = u0.shape
+    which = C.c_int(0)
+    p = C.byref(params) if params is not None else None
+    call("hyd_cuda_iterate_gray_scott_f64", ptr(u0), ptr(v0), ptr(u1), ptr(v1), h, w, p, steps, C.byref(which),
+         stream_handle(stream))
+    return (u1, v1) if which.value else (u0, v0)
 
 
 def selftest_dadd(x, y):

@@ -168,6 +168,26 @@ int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t
  * unit's x[i] + y[i] (round to nearest even).  No counterpart in the
  * reference; for tests. */
 int hyd_cuda_selftest_dadd(const double* x, const double* y, double* emu, double* hw, int64_t n, void* stream);
+/* ---- the other iterate loops ---------------------------------------------------
+ * jacobi_1d (examples/jacobi_1d.hyd:4): out[i] = (in[i-1] + in[i] + in[i+1]) / 3.0
+ * with clamped neighbours, float64, bit-identical to the C backend. */
+int hyd_cuda_jacobi1d_f64(const double* in, double* out, int64_t n, void* stream);
+int hyd_cuda_iterate_jacobi1d_f64(double* buf0, double* buf1, int64_t n, int64_t iters, int* final_buf,
+                                  void* stream);
+/* Gray-Scott reaction-diffusion (demo/gray_scott/gray_scott.hyd:47-73): one step
+ * of U and V on an h x w periodic grid, each expression in the program's order
+ * (bit-identical to the C backend).  params NULL = the demo's constants
+ * (du 0.21, dv 0.105, feed 0.0545, kill 0.0620, dt 1.0).  The iterate form
+ * ping-pongs (u0, v0) <-> (u1, v1); *final_buf = 1 when the result is in
+ * (u1, v1).  Like the stencil iterate, a non-default stream runs a cached
+ * captured graph. */
+typedef struct {
+    double du, dv, feed, kill, dt;
+} hyd_gray_scott_t;
+int hyd_cuda_gray_scott_step_f64(const double* u, const double* v, double* u_out, double* v_out, int64_t h,
+                                 int64_t w, const hyd_gray_scott_t* params, void* stream);
+int hyd_cuda_iterate_gray_scott_f64(double* u0, double* v0, double* u1, double* v1, int64_t h, int64_t w,
+                                    const hyd_gray_scott_t* params, int64_t steps, int* final_buf, void* stream);
 /* Releases the cached iterate graphs (also done by hyd_cuda_cleanup). */
 void hyd_cuda_stencil_release_graphs(void);
 /* Same, with an explicit kernel variant instead of the autotuned one
@@ -386,6 +406,10 @@ hyd_array_t* hyd_cuda_array_alloc(hyd_tuple_t shape, size_t elem_size);
  * a message and exit(1) on failure (runtime/hydrangea_runtime.h:322-328).
  * Returned arrays are owned by the caller (free with hyd_array_free). */
 hyd_array_t* hyd_export_weighted_histogram(hyd_array_t* data, int64_t bins);
+/* demo/gray_scott's procedure (gray_scott.hyd:80; demo/gray_scott/main.cpp:85
+ * calls it): V after 5000 steps on the demo's 256 x 256 grid from its initial
+ * fields. */
+hyd_array_t* hyd_export_gray_scott(void);
 double hyd_export_dot(hyd_array_t* xs, hyd_array_t* ys);
 
 #ifdef __cplusplus

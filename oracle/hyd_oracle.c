@@ -384,6 +384,67 @@ void orc_stencil1d_box3_i64(const int64_t* in, int64_t* out, int64_t n) {
     }
 }
 
+/* 1-D clamp Jacobi `stencil clamp (fn acc => (acc (-1) +. acc 0 +. acc 1) /. 3.0)`
+ * (examples/jacobi_1d.hyd:4): the clamped split-region loop of
+ * Lowering.hs:1932-2035 in one dimension; left-to-right sum, then the IEEE
+ * division.                                                                  */
+void orc_stencil1d_jacobi3_f64(const double* in, double* out, int64_t n) {
+    for (int64_t i = 0; i < n; i++) {
+        int64_t l = orc_clamp(i - 1, n), r = orc_clamp(i + 1, n);
+        double s = in[l] + in[i];
+        s = s + in[r];
+        out[i] = s / 3.0;
+    }
+}
+
+int orc_iterate_stencil1d_jacobi3_f64(double* buf0, double* buf1, int64_t n, int64_t iters) {
+    double* cur = buf0;
+    double* nxt = buf1;
+    for (int64_t t = 0; t < iters; t++) {
+        orc_stencil1d_jacobi3_f64(cur, nxt, n);
+        double* tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    return cur == buf0 ? 0 : 1;
+}
+
+/* One Gray-Scott step (demo/gray_scott/gray_scott.hyd:47-73): periodic
+ * 5-point Laplacians of U and V through `imod`, the reaction terms, and the
+ * updates, each expression evaluated left to right exactly as written:
+ *   lap  = u[im1,j] + u[ip1,j] + u[i,jm1] + u[i,jp1] - 4*u_ij
+ *   uvv  = u_ij * v_ij * v_ij
+ *   u'   = u_ij + dt * (du*lap - uvv + feed*(1 - u_ij))
+ *   v'   = v_ij + dt * (dv*lapv + uvv - (feed + kill)*v_ij)                  */
+void orc_gray_scott_step_f64(const double* u, const double* v, double* un, double* vn, int64_t h, int64_t w,
+                             double du, double dv, double feed, double kill, double dt) {
+    for (int64_t i = 0; i < h; i++) {
+        int64_t im1 = (i - 1 + h) % h, ip1 = (i + 1) % h;
+        for (int64_t j = 0; j < w; j++) {
+            int64_t jm1 = (j - 1 + w) % w, jp1 = (j + 1) % w;
+            double uij = u[i * w + j], vij = v[i * w + j];
+            double lu = u[im1 * w + j] + u[ip1 * w + j];
+            lu = lu + u[i * w + jm1];
+            lu = lu + u[i * w + jp1];
+            lu = lu - 4.0 * uij;
+            double lv = v[im1 * w + j] + v[ip1 * w + j];
+            lv = lv + v[i * w + jm1];
+            lv = lv + v[i * w + jp1];
+            lv = lv - 4.0 * vij;
+            double uvv = uij * vij;
+            uvv = uvv * vij;
+            double tu = du * lu;
+            tu = tu - uvv;
+            tu = tu + feed * (1.0 - uij);
+            un[i * w + j] = uij + dt * tu;
+            double tv = dv * lv;
+            tv = tv + uvv;
+            tv = tv - (feed + kill) * vij;
+            vn[i * w + j] = vij + dt * tv;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------------- */
 /* scan / scan_inclusive / scanr / scanr_inclusive with (+)
  * (Lowering.hs:3563-3612, lowerScanFamily): a serial LoopFold; the reverse

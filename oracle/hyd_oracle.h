@@ -49,6 +49,10 @@ void orc_stencil2d_f64(int kind, const double* in, double* out, int64_t h, int64
 int orc_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
                               int64_t iters);
 void orc_stencil1d_box3_i64(const int64_t* in, int64_t* out, int64_t n);
+void orc_stencil1d_jacobi3_f64(const double* in, double* out, int64_t n);
+int orc_iterate_stencil1d_jacobi3_f64(double* buf0, double* buf1, int64_t n, int64_t iters);
+void orc_gray_scott_step_f64(const double* u, const double* v, double* un, double* vn, int64_t h, int64_t w,
+                             double du, double dv, double feed, double kill, double dt);
 
 /* ---- scan family and segmented reduce ------------------------------------ */
 void orc_scan_i64(const int64_t* in, int64_t* out, int64_t n, int64_t init,

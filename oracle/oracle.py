@@ -45,6 +45,10 @@ def lib():
             "orc_stencil2d_f64": (None, [C.c_int, _f64p, _f64p, _i64, _i64]),
             "orc_iterate_stencil2d_f64": (C.c_int, [C.c_int, _f64p, _f64p, _i64, _i64, _i64]),
             "orc_stencil1d_box3_i64": (None, [_i64p, _i64p, _i64]),
+            "orc_stencil1d_jacobi3_f64": (None, [_f64p, _f64p, _i64]),
+            "orc_iterate_stencil1d_jacobi3_f64": (C.c_int, [_f64p, _f64p, _i64, _i64]),
+            "orc_gray_scott_step_f64": (None, [_f64p, _f64p, _f64p, _f64p, _i64, _i64, C.c_double, C.c_double,
+                                                C.c_double, C.c_double, C.c_double]),
             "orc_scan_i64": (None, [_i64p, _i64p, _i64, _i64, C.c_int, C.c_int]),
             "orc_scan_f64": (None, [_f64p, _f64p, _i64, C.c_double, C.c_int, C.c_int]),
             "orc_segmented_reduce_i64": (C.c_int, [_i64p, _i64, _i64p, _i64, _i64, _i64p]),
@@ -156,6 +160,31 @@ def iterate_stencil2d(kind, grid, iters):
     h, w = b0.shape
     which = lib().orc_iterate_stencil2d_f64(kind, b0.reshape(-1), b1.reshape(-1), h, w, iters)
     return b0 if which == 0 else b1
+
+
+def jacobi1d(x, iters=1):
+    """iters clamped 3-point Jacobi steps (examples/jacobi_1d.hyd)."""
+    b0 = np.ascontiguousarray(x, dtype=np.float64).copy()
+    b1 = np.empty_like(b0)
+    which = lib().orc_iterate_stencil1d_jacobi3_f64(b0, b1, len(b0), iters)
+    return b0 if which == 0 else b1
+
+
+# demo/gray_scott/gray_scott.hyd:19-25
+GRAY_SCOTT = dict(du=0.21, dv=0.105, feed=0.0545, kill=0.0620, dt=1.0)
+
+
+def gray_scott(u, v, steps=1, du=0.21, dv=0.105, feed=0.0545, kill=0.0620, dt=1.0):
+    u = np.ascontiguousarray(u, dtype=np.float64).copy()
+    v = np.ascontiguousarray(v, dtype=np.float64).copy()
+    h, w = u.shape
+    un, vn = np.empty_like(u), np.empty_like(v)
+    for _ in range(steps):
+        lib().orc_gray_scott_step_f64(u.reshape(-1), v.reshape(-1), un.reshape(-1), vn.reshape(-1), h, w,
+                                      du, dv, feed, kill, dt)
+        u, un = un, u
+        v, vn = vn, v
+    return u, v
 
 
 def scan_i64(x, init=0, reverse=False, inclusive=False):

@@ -16,7 +16,8 @@ def _check(hc, x, y, dev):
     xt, yt = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
     emu, hw = hc.selftest_dadd(xt, yt)
     assert np.array_equal(_bits(emu), _bits(hw))
-    ref = x + y
+    with np.errstate(over="ignore"):
+        ref = x + y
     fin = np.isfinite(ref) | np.isinf(ref)
     assert np.array_equal(_bits(hw)[fin], ref.view(np.uint64)[fin])
 
@@ -42,10 +43,12 @@ def test_random_positive_normals_every_exponent_gap(hc, dev):
 def test_ties_carries_and_overflow(hc, dev):
     one = 1.0
     ulp = np.spacing(1.0)
-    xs = [one, one + ulp, one + 2 * ulp, 2.0 - ulp, 1.5, np.finfo(np.float64).max,
-          np.finfo(np.float64).max, 1e308, 0.5, 3.0, 2.0 ** 1023, 1.0]
-    ys = [ulp / 2, ulp / 2, ulp / 2, ulp / 2, 1.5, np.finfo(np.float64).max,
-          np.spacing(np.finfo(np.float64).max) / 2, 1e308, 0.5 - ulp / 4, ulp, 2.0 ** 1023, 2.0 ** -1022]
+    big = np.finfo(np.float64).max
+    half_ulp_big = 2.0 ** 970  # half an ulp of the largest double
+    xs = [one, one + ulp, one + 2 * ulp, 2.0 - ulp, 1.5, big,
+          big, 1e308, 0.5, 3.0, 2.0 ** 1023, 1.0]
+    ys = [ulp / 2, ulp / 2, ulp / 2, ulp / 2, 1.5, big,
+          half_ulp_big, 1e308, 0.5 - ulp / 4, ulp, 2.0 ** 1023, 2.0 ** -1022]
     x, y = np.array(xs), np.array(ys)
     _check(hc, x, y, dev)
     # exhaustive low-bit patterns around ties: x = 1 + k ulp, y = j * 2^-56

@@ -243,3 +243,19 @@ def test_hist_privatized_equals_atomic(orc):
 def test_hist_rejects_negative_routes(orc):
     with pytest.raises(ValueError):
         orc.weighted_hist(np.array([-3, 5], dtype=np.int64), 4)
+
+
+def test_jacobi_1d_example_and_clamp(orc):
+    """examples/jacobi_1d.hyd: three steps over ones stay ones; one step of
+    1..5 is the clamped 3-point sums of StencilSpec.hs (4, 6, 9, 12, 14) / 3."""
+    import numpy as np
+    assert orc.jacobi1d(np.ones(5), 3).tolist() == [1.0] * 5
+    assert orc.jacobi1d(np.arange(1.0, 6.0), 1).tolist() == [4.0 / 3.0, 2.0, 3.0, 4.0, 14.0 / 3.0]
+
+
+def test_gray_scott_fixed_point(orc):
+    """U = 1, V = 0 is a fixed point of the Gray-Scott step (no reaction, no
+    diffusion), exactly."""
+    import numpy as np
+    u, v = orc.gray_scott(np.ones((9, 7)), np.zeros((9, 7)), 10)
+    assert (u == 1.0).all() and (v == 0.0).all()
