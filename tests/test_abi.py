@@ -1,8 +1,12 @@
 """The C-ABI library loads, exports every symbol include/*.h declares, and
 rejects bad arguments before touching a GPU (runs without one)."""
 import ctypes as C
+import os
+import sys
 
 import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_library_exports_header_symbols(hc):
@@ -52,3 +56,28 @@ def test_server_requires_device_or_rejects_cleanly(hc):
     if not torch.cuda.is_available():
         h = C.c_void_p()
         assert L.hyd_cuda_server_create(None, C.byref(h)) == hc.ERR_NO_DEVICE
+
+
+def test_gray_scott_demo_host_links_unchanged(tmp_path):
+    """The reference's embedding demo host links against the runtime without a
+    change: its generated header (CodegenC.hs:427-460 form) only needs to
+    declare hyd_export_gray_scott.  Link only -- there is no GPU to run it."""
+    import shutil
+    import subprocess
+    sys.path.insert(0, ROOT)
+    from oracle import build as ob
+    root = os.environ.get("HYD_REFERENCE_ROOT", ob.DEFAULT_REFERENCE_ROOT)
+    main = os.path.join(root, "demo", "gray_scott", "main.cpp")
+    if not os.path.exists(main) or shutil.which("g++") is None:
+        pytest.skip("reference demo sources not present")
+    (tmp_path / "gray_scott.h").write_text(
+        "#ifndef HYDRANGEA_EXPORT_GRAY_SCOTT_H\n#define HYDRANGEA_EXPORT_GRAY_SCOTT_H\n"
+        '#include "hydrangea_runtime.h"\n#include "hyd_cuda.h"\n#endif\n')
+    pkg = os.path.join(ROOT, "hydrangea-compiler_gb300")
+    out = tmp_path / "gs_demo"
+    cmd = ["g++", "-O1", "-fopenmp", "-I", str(tmp_path), "-I", os.path.join(root, "runtime"),
+           "-I", os.path.join(ROOT, "oracle"), "-I", os.path.join(ROOT, "include"), main,
+           "-L", pkg, "-lhyd_cuda", "-Wl,-rpath," + pkg, "-o", str(out)]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert out.exists()
