@@ -41,7 +41,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="histogram",
-                   choices=["histogram", "dot", "heat", "jacobi1d", "gray_scott", "batched", "serve"],
+                   choices=["histogram", "dot", "map_chain", "heat", "jacobi1d", "gray_scott", "batched", "serve"],
                    help="histogram: the headline line; the others run one configuration of the suite alone "
                         "(its JSON object on one line; --steps sets its repetitions / heat iterations)")
     p.add_argument("--variant", type=int, default=-1,
@@ -460,6 +460,31 @@ def suite_heat(hc, torch, peak, iters=1000, variant=-1):
                                  "the 6 per-point operations as exact integer-pipe additions" % emu}}
 
 
+def suite_map_chain(hc, torch, peak, steps=20):
+    """bench/map_chain/map_chain.hyd: reduce (+) over generate (i/n) -> x*x ->
+    x-0.5 -> x*2+1, n = 2^27, one fused run-time-compiled kernel (no memory
+    traffic: the chain is generated)."""
+    import math
+    import numpy as np
+    n = 1 << 27
+    body = "double s = (double)i / %d.0; double a = s * s; double b = a - 0.5; v = b * 2.0 + 1.0;" % n
+    _, ssum = hc.map_f64(body, [], n=n, want_sum=True)  # compiles, warms up
+    s = torch.cuda.current_stream()
+    e0, e1 = _events(torch, s)
+    e0.record(s)
+    for _ in range(steps):
+        hc.map_f64(body, [], n=n, want_sum=True)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    # closed form of the exact sum for the accuracy report: sum 2 (i/n)^2 = 2 (n-1)(2n-1) / (6n)
+    exact = 2.0 * (n - 1) * (2 * n - 1) / (6.0 * n)
+    return {"config": "map_chain reduce(+) (map (x*2+1) (map (x-0.5) (map (x*x) (generate [n] (i/n))))), n=2^27 f64",
+            "ms": round(ms, 4), "Gelem_s": round(n / (ms / 1e3) / 1e9, 2), "sum": ssum.item(),
+            "rel_err_vs_exact": abs(ssum.item() - exact) / abs(exact),
+            "note": "compute only (generated input); one IEEE division per element on GB300's FP64 unit bounds it"}
+
+
 def suite_jacobi1d(hc, torch, peak, iters=100):
     """jacobi_1d (examples/jacobi_1d.hyd) over n = 2^25 float64, a captured graph."""
     n = 1 << 25
@@ -675,7 +700,8 @@ def suite_serve(hc, torch, peak, nreq=100_000, lam=20_000.0):
 
 def run_suite(hc, torch, args, peak):
     out = {}
-    for name, fn in (("dot", suite_dot), ("heat_2d", suite_heat), ("jacobi_1d", suite_jacobi1d),
+    for name, fn in (("dot", suite_dot), ("map_chain", suite_map_chain), ("heat_2d", suite_heat),
+                     ("jacobi_1d", suite_jacobi1d),
                      ("gray_scott", suite_gray_scott), ("batched_coo_csr_spmv", suite_batched),
                      ("serving", lambda a, b, c: suite_serve(a, b, c, nreq=args.serve_requests))):
         t = time.perf_counter()
@@ -765,6 +791,8 @@ def run_one(args):
         res = suite_dot(hc, torch, peak, steps=args.steps)
     elif args.workload == "heat":
         res = suite_heat(hc, torch, peak, iters=args.steps, variant=args.variant)
+    elif args.workload == "map_chain":
+        res = suite_map_chain(hc, torch, peak, steps=args.steps)
     elif args.workload == "jacobi1d":
         res = suite_jacobi1d(hc, torch, peak, iters=args.steps)
     elif args.workload == "gray_scott":

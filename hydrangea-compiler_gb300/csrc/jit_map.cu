@@ -1,0 +1,252 @@
+// jit_map.cu -- fused map / zipwith / generate chains compiled at run time.
+//
+// The C backend turns a fused chain such as
+//   reduce (+) 0.0 (map (fn x => x *. 2.0 +. 1.0) (map (fn x => x -. 0.5)
+//     (map (fn x => x *. x) (generate [n] (fn [i] => float_of i /. float_of n)))))
+// (bench/map_chain/map_chain.hyd) into one loop whose body evaluates the
+// composed element expression (CodegenC.hs:1328-1353 for the reduced form).
+// Here the generated element body -- C statements over the inputs' elements
+// x0..x7 and the index i that assign `v` -- is compiled once per body and
+// device with NVRTC into a kernel that:
+//   * walks the elements as a grid-stride loop over pairs, with 128-bit
+//     (double2) loads and stores when every pointer is 16-byte aligned;
+//   * evaluates the body with IEEE round-to-nearest operations and no
+//     contraction (--fmad=false), so each element equals the C backend's;
+//   * optionally writes the elements and/or reduces them with (+): per-thread
+//     sums, a fixed shuffle tree per block, block partials combined in block
+//     order by the last block -- the same bits on every run.
+// NVRTC is loaded with dlopen on first use; without it the call reports
+// HYD_CUDA_ERR_UNSUPPORTED.
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "hyd_common.cuh"
+
+namespace hyd {
+
+struct Nvrtc {
+    bool tried = false, ok = false;
+    decltype(&nvrtcCreateProgram) create = nullptr;
+    decltype(&nvrtcCompileProgram) compile = nullptr;
+    decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+    decltype(&nvrtcGetProgramLog) log = nullptr;
+    decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+    decltype(&nvrtcGetCUBIN) cubin = nullptr;
+    decltype(&nvrtcDestroyProgram) destroy = nullptr;
+};
+
+static std::mutex g_jit_mu;
+static Nvrtc g_nvrtc;
+
+static bool load_nvrtc_locked() {
+    if (g_nvrtc.tried) return g_nvrtc.ok;
+    g_nvrtc.tried = true;
+    std::vector<std::string> names = {"libnvrtc.so.13", "libnvrtc.so"};
+    if (const char* home = getenv("CUDA_HOME")) names.push_back(std::string(home) + "/lib64/libnvrtc.so.13");
+    names.push_back("/usr/local/cuda/lib64/libnvrtc.so.13");  // the toolkit's default install location
+    void* h = nullptr;
+    for (const std::string& n : names)
+        if ((h = dlopen(n.c_str(), RTLD_NOW | RTLD_LOCAL)) != nullptr) break;
+    if (!h) return false;
+    g_nvrtc.create = (decltype(&nvrtcCreateProgram))dlsym(h, "nvrtcCreateProgram");
+    g_nvrtc.compile = (decltype(&nvrtcCompileProgram))dlsym(h, "nvrtcCompileProgram");
+    g_nvrtc.log_size = (decltype(&nvrtcGetProgramLogSize))dlsym(h, "nvrtcGetProgramLogSize");
+    g_nvrtc.log = (decltype(&nvrtcGetProgramLog))dlsym(h, "nvrtcGetProgramLog");
+    g_nvrtc.cubin_size = (decltype(&nvrtcGetCUBINSize))dlsym(h, "nvrtcGetCUBINSize");
+    g_nvrtc.cubin = (decltype(&nvrtcGetCUBIN))dlsym(h, "nvrtcGetCUBIN");
+    g_nvrtc.destroy = (decltype(&nvrtcDestroyProgram))dlsym(h, "nvrtcDestroyProgram");
+    g_nvrtc.ok = g_nvrtc.create && g_nvrtc.compile && g_nvrtc.log_size && g_nvrtc.log && g_nvrtc.cubin_size &&
+                 g_nvrtc.cubin && g_nvrtc.destroy;
+    return g_nvrtc.ok;
+}
+
+constexpr int kMapMaxInputs = 8;
+constexpr int kMapThreads = 256;
+
+// Kernel source for `body` over `nin` inputs.
+static std::string map_source(const std::string& body, int nin) {
+    std::string s;
+    s += "__device__ __forceinline__ double hyd_elem(long long i";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += ", double x" + std::to_string(k);
+    s += ") {\n  double v = 0.0;\n  (void)i;\n";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += "  (void)x" + std::to_string(k) + ";\n";
+    s += "  {\n" + body + "\n  }\n  return v;\n}\n";
+    s += "extern \"C\" __global__ void __launch_bounds__(256) hyd_map_kernel(";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += "const double* __restrict__ p" + std::to_string(k) + ", ";
+    s += "long long n, double* __restrict__ out, double* __restrict__ partials, unsigned int* counter, "
+         "double* __restrict__ sum, int vec) {\n"
+         "  double acc = 0.0;\n"
+         "  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
+         "  const long long nt = (long long)gridDim.x * blockDim.x;\n"
+         "  if (vec) {\n"
+         "    const long long np = n >> 1;\n"
+         "    for (long long q = t; q < np; q += nt) {\n"
+         "      const long long i = 2 * q;\n";
+    for (int k = 0; k < kMapMaxInputs; ++k) {
+        const std::string ks = std::to_string(k);
+        if (k < nin) s += "      const double2 a" + ks + " = ((const double2*)p" + ks + ")[q];\n";
+        else s += "      const double2 a" + ks + " = make_double2(0.0, 0.0);\n";
+    }
+    s += "      const double v0 = hyd_elem(i";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += ", a" + std::to_string(k) + ".x";
+    s += ");\n      const double v1 = hyd_elem(i + 1";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += ", a" + std::to_string(k) + ".y";
+    s += ");\n"
+         "      if (out) ((double2*)out)[q] = make_double2(v0, v1);\n"
+         "      acc += v0;\n"
+         "      acc += v1;\n"
+         "    }\n"
+         "    if (t == 0 && (n & 1)) {\n"
+         "      const long long i = n - 1;\n"
+         "      const double v = hyd_elem(i";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += k < nin ? ", p" + std::to_string(k) + "[i]" : ", 0.0";
+    s += ");\n"
+         "      if (out) out[i] = v;\n"
+         "      acc += v;\n"
+         "    }\n"
+         "  } else {\n"
+         "    for (long long i = t; i < n; i += nt) {\n"
+         "      const double v = hyd_elem(i";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += k < nin ? ", p" + std::to_string(k) + "[i]" : ", 0.0";
+    s += ");\n"
+         "      if (out) out[i] = v;\n"
+         "      acc += v;\n"
+         "    }\n"
+         "  }\n"
+         "  if (sum == 0) return;\n"
+         // fixed shuffle tree per warp, warps in order per block, blocks in order by the last block
+         "  __shared__ double wsum[8];\n"
+         "  __shared__ bool last;\n"
+         "  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);\n"
+         "  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;\n"
+         "  __syncthreads();\n"
+         "  if (threadIdx.x == 0) {\n"
+         "    double b = 0.0;\n"
+         "    for (int w = 0; w < 8; ++w) b += wsum[w];\n"
+         "    partials[blockIdx.x] = b;\n"
+         "    __threadfence();\n"
+         "    last = atomicAdd(counter, 1u) == gridDim.x - 1;\n"
+         "  }\n"
+         "  __syncthreads();\n"
+         "  if (last && threadIdx.x == 0) {\n"
+         "    __threadfence();\n"
+         "    double s = 0.0;\n"
+         "    for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(partials + b);\n"
+         "    *sum = s;\n"
+         "    *counter = 0u;\n"
+         "  }\n"
+         "}\n";
+    return s;
+}
+
+struct MapKernel {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t kern = nullptr;
+};
+static std::map<std::tuple<int, int, std::string>, MapKernel> g_map_kernels;
+
+static int compile_map(Device* d, const std::string& body, int nin, MapKernel* out) {
+    std::lock_guard<std::mutex> lock(g_jit_mu);
+    auto key = std::make_tuple(d->id, nin, body);
+    auto it = g_map_kernels.find(key);
+    if (it != g_map_kernels.end()) {
+        *out = it->second;
+        return HYD_CUDA_OK;
+    }
+    if (!load_nvrtc_locked()) return set_error(HYD_CUDA_ERR_UNSUPPORTED, "map_f64: NVRTC library not found");
+    int major = 0, minor = 0;
+    HYD_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, d->id));
+    HYD_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, d->id));
+    const std::string src = map_source(body, nin);
+    nvrtcProgram prog = nullptr;
+    if (g_nvrtc.create(&prog, src.c_str(), "hyd_map.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        return set_error(HYD_CUDA_ERR_CUDA, "map_f64: nvrtcCreateProgram failed");
+    const std::string arch = "--gpu-architecture=sm_" + std::to_string(major) + std::to_string(minor);
+    const char* opts[] = {arch.c_str(), "--fmad=false", "--std=c++17"};
+    const nvrtcResult cr = g_nvrtc.compile(prog, 3, opts);
+    if (cr != NVRTC_SUCCESS) {
+        size_t n = 0;
+        g_nvrtc.log_size(prog, &n);
+        std::string log(n, '\0');
+        if (n) g_nvrtc.log(prog, &log[0]);
+        g_nvrtc.destroy(&prog);
+        return set_error(HYD_CUDA_ERR_INVALID, "map_f64: the element body does not compile: %.400s", log.c_str());
+    }
+    size_t cn = 0;
+    g_nvrtc.cubin_size(prog, &cn);
+    std::vector<char> cubin(cn);
+    g_nvrtc.cubin(prog, cubin.data());
+    g_nvrtc.destroy(&prog);
+    MapKernel mk;
+    HYD_CUDA_TRY(cudaLibraryLoadData(&mk.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+    const cudaError_t ke = cudaLibraryGetKernel(&mk.kern, mk.lib, "hyd_map_kernel");
+    if (ke != cudaSuccess) {
+        cudaLibraryUnload(mk.lib);
+        return set_error(HYD_CUDA_ERR_CUDA, "map_f64: %s", cudaGetErrorString(ke));
+    }
+    g_map_kernels[key] = mk;
+    *out = mk;
+    return HYD_CUDA_OK;
+}
+
+void release_map_kernels() {
+    std::lock_guard<std::mutex> lock(g_jit_mu);
+    for (auto& kv : g_map_kernels) cudaLibraryUnload(kv.second.lib);
+    g_map_kernels.clear();
+}
+
+}  // namespace hyd
+
+using namespace hyd;
+
+extern "C" int hyd_cuda_map_f64(const char* body, const double* const* inputs, int ninputs, int64_t n, double* out,
+                                double* sum, void* stream) {
+    HYD_CHECK_ARG(body != nullptr && *body, "map_f64: empty element body");
+    HYD_CHECK_ARG(ninputs >= 0 && ninputs <= kMapMaxInputs, "map_f64: 0..%d inputs", kMapMaxInputs);
+    HYD_CHECK_ARG(n >= 0, "map_f64: negative length");
+    HYD_CHECK_ARG(ninputs == 0 || inputs != nullptr, "map_f64: null input table");
+    for (int k = 0; k < ninputs; ++k) HYD_CHECK_ARG(n == 0 || inputs[k] != nullptr, "map_f64: null input %d", k);
+    cudaStream_t s = as_stream(stream);
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    MapKernel mk;
+    HYD_TRY(compile_map(d, body, ninputs, &mk));  // compile errors surface even for n == 0
+    if (n == 0) {
+        if (sum) HYD_CUDA_TRY(cudaMemsetAsync(sum, 0, sizeof(double), s));
+        return HYD_CUDA_OK;
+    }
+    bool vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    const double* p[kMapMaxInputs] = {nullptr};
+    for (int k = 0; k < ninputs; ++k) {
+        p[k] = inputs[k];
+        vec = vec && (reinterpret_cast<uintptr_t>(p[k]) & 15) == 0;
+    }
+    const int64_t pairs = (n + 1) / 2;
+    int64_t grid = (pairs + kMapThreads - 1) / kMapThreads;
+    const int64_t cap = (int64_t)d->sm_count * 8;
+    if (grid > cap) grid = cap;
+    unsigned* counters = nullptr;
+    void* scratch = nullptr;
+    HYD_TRY(workspace(s, (size_t)grid * sizeof(double), &counters, &scratch));
+    unsigned* counter = counters + 200;  // reset by the kernel's last block
+    double* partials = static_cast<double*>(scratch);
+    long long nn = n;
+    int v = vec ? 1 : 0;
+    void* args[kMapMaxInputs + 6];
+    for (int k = 0; k < kMapMaxInputs; ++k) args[k] = &p[k];
+    args[kMapMaxInputs + 0] = &nn;
+    args[kMapMaxInputs + 1] = &out;
+    args[kMapMaxInputs + 2] = &partials;
+    args[kMapMaxInputs + 3] = &counter;
+    args[kMapMaxInputs + 4] = &sum;
+    args[kMapMaxInputs + 5] = &v;
+    HYD_CUDA_TRY(cudaLaunchKernel((const void*)mk.kern, dim3((unsigned)grid), dim3(kMapThreads), args, 0, s));
+    return HYD_CUDA_OK;
+}

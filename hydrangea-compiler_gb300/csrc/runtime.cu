@@ -11,6 +11,10 @@
 #include "hyd_common.cuh"
 
 namespace hyd {
+void release_map_kernels();  // jit_map.cu
+}
+
+namespace hyd {
 
 static thread_local char g_last_error[1024] = "";
 
@@ -190,6 +194,7 @@ extern "C" void hyd_cuda_stencil_release_graphs(void);
 
 void hyd_cuda_cleanup(void) {
     hyd_cuda_stencil_release_graphs();
+    release_map_kernels();
     std::lock_guard<std::mutex> lock(g_devices_mu);
     int cur = 0;
     if (cudaGetDevice(&cur) != cudaSuccess) cur = 0;

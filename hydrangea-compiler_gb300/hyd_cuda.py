@@ -89,6 +89,7 @@ SIGNATURES = {
     "hyd_export_weighted_histogram": (_p, [_p, _i64]),
     "hyd_export_dot": (_d, [_p, _p]),
     "hyd_export_gray_scott": (_p, []),
+    "hyd_cuda_map_f64": (_i, [C.c_char_p, _p, _i, _i64, _p, _p, _p]),
     "hyd_cuda_jacobi1d_f64": (_i, [_p, _p, _i64, _p]),
     "hyd_cuda_iterate_jacobi1d_f64": (_i, [_p, _p, _i64, _i64, C.POINTER(C.c_int), _p]),
     "hyd_cuda_gray_scott_step_f64": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _p]),
@@ -261,6 +262,21 @@ def iterate_stencil2d(kind, buf0, buf1, iters, stream=None, variant=-1):
     call("hyd_cuda_iterate_stencil2d_f64_variant", kind, ptr(buf0), ptr(buf1), h, w, iters, variant,
          C.byref(fb), stream_handle(stream))
     return buf0 if fb.value == 0 else buf1
+
+
+def map_f64(body, inputs, n=None, out=None, want_sum=False, stream=None):
+    """Fused element chain: `body` (C statements assigning v from x0.., i) over
+    device tensors `inputs`; returns (out, sum or None)."""
+    import torch
+    n = inputs[0].numel() if n is None else n
+    table = (C.c_void_p * max(len(inputs), 1))(*[t.data_ptr() for t in inputs])
+    s = None
+    if want_sum:
+        dev = inputs[0].device if inputs else torch.device("cuda")
+        s = torch.zeros(1, dtype=torch.float64, device=dev)
+    call("hyd_cuda_map_f64", body.encode(), C.cast(table, C.c_void_p), len(inputs), n,
+         ptr(out) if out is not None else None, ptr(s) if s is not None else None, stream_handle(stream))
+    return out, s
 
 
 class GrayScott(C.Structure):

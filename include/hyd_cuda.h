@@ -168,6 +168,22 @@ int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t
  * unit's x[i] + y[i] (round to nearest even).  No counterpart in the
  * reference; for tests. */
 int hyd_cuda_selftest_dadd(const double* x, const double* y, double* emu, double* hw, int64_t n, void* stream);
+/* ---- fused map / zipwith / generate chains -------------------------------------
+ * The element loop of a fused chain (bench/map_chain/map_chain.hyd; the C
+ * backend's loop body, CodegenC.hs:1328-1353 for the reduced form) with its
+ * body given as generated C statements over x0..x{ninputs-1} (element i of
+ * inputs[k], double), i (int64 index) and assigning the double `v`, e.g.
+ *   "double s = (double)i / 4096.0; double a = s * s; v = (a - 0.5) * 2.0 + 1.0;"
+ * inputs: HOST array of ninputs (<= 8) device pointers.  out (n doubles, may be
+ * NULL) receives the elements, each bit-identical to the C backend (IEEE
+ * round-to-nearest, no contraction); sum (one device double, may be NULL)
+ * receives their (+) reduction in a fixed order (run-to-run identical).
+ * Compiled once per (device, body, ninputs) at run time with NVRTC
+ * (HYD_CUDA_ERR_UNSUPPORTED if the NVRTC library is absent; a body that does
+ * not compile is HYD_CUDA_ERR_INVALID with the compiler's message). */
+int hyd_cuda_map_f64(const char* body, const double* const* inputs, int ninputs, int64_t n, double* out,
+                     double* sum, void* stream);
+
 /* ---- the other iterate loops ---------------------------------------------------
  * jacobi_1d (examples/jacobi_1d.hyd:4): out[i] = (in[i-1] + in[i] + in[i+1]) / 3.0
  * with clamped neighbours, float64, bit-identical to the C backend. */
