@@ -164,6 +164,21 @@ def test_plan_reports_strategy_and_launches(hc, dev):
     assert hc.weighted_histogram_plan(1 << 27, 1 << 20) == (hc.SCATTER_GLOBAL, 1)
 
 
+@pytest.mark.parametrize("bins,bound", [(65536, 1 << 14), (65536, 1 << 20), (40000, 1 << 20), (131072, 1 << 40),
+                                        (20000, 1 << 20)])
+def test_partition_skew_widths_and_range_counts(hc, orc, dev, bins, bound):
+    # 12M elements: with bound 2^14 every element lands in the first bin range
+    # (one apply range gets every CTA); bound 2^40 stages every tile as 8-byte
+    # records; 131072 bins take the eight-range staging path; one wide tile
+    # sits mid-stream among narrow ones
+    n = 12_000_017
+    data = _data(hc, n, dev, seed=21, bound=bound)
+    data[5_000_000:5_004_096] = _data(hc, 4096, dev, seed=22, bound=1 << 62)
+    for d in (data, data[1:]):
+        assert np.array_equal(_run(hc, d, bins, hc.SCATTER_PARTITION, dev),
+                              orc.weighted_hist(d.cpu().numpy(), bins))
+
+
 @pytest.mark.parametrize("bins", [65536, 40000])
 def test_partition_mixed_record_widths(hc, orc, dev, bins):
     # tiles of small values are staged as 4-byte records, tiles holding a value
