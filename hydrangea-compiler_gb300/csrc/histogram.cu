@@ -476,7 +476,10 @@ constexpr int kPartQueueWord = 64;
 
 // Pass 1.  Tiles stream through three shared-memory buffers: one thread
 // bulk-loads tile i + 2 while tile i is grouped (mbarrier completion, bounded
-// waits), and the grouped tile is bulk-stored from the same buffer.  Every
+// waits), and the grouped tile is bulk-stored from the same buffer.  The load
+// of tile i + 2 goes into the buffer of tile i - 1 and is issued at the end of
+// iteration i, right after tile i's store: by then the store of tile i - 1 has
+// long read its buffer, so the wait for that never holds up the block.  Every
 // thread counts its eight elements per range in packed 16-bit fields (NW words
 // of two ranges); one block-wide exclusive scan of those words gives each
 // thread its offset inside every range; the elements, held in registers, are
@@ -518,13 +521,6 @@ __global__ void __launch_bounds__(kPartThreads, kPartCtasPerSm)
     bool timed_out = false;
     for (; tile < ntiles; tile += gridDim.x, ++it) {
         const int buf = (int)(it % kPartBufs);
-        const int64_t ahead = tile + (int64_t)(kPartBufs - 1) * gridDim.x;
-        if (threadIdx.x == 0 && ahead < ntiles) {
-            // the buffer of tile i - 1: its bulk store must have read it
-            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(ahead, (int)((it + kPartBufs - 1) % kPartBufs));
-        }
         // one thread polls (acquire on the mbarrier phase); the block barrier
         // then orders the landed tile before every thread's reads
         const bool arrived = threadIdx.x == 0 ? mbar_wait_bounded(bar0 + 8 * buf, (it / kPartBufs) & 1u) : true;
@@ -727,25 +723,34 @@ __global__ void __launch_bounds__(kPartThreads, kPartCtasPerSm)
             const unsigned esz = wide ? 8u : 4u;
             const unsigned all = rstart[P] * esz;
             const unsigned sbytes = all & ~15u;
-            if (sbytes) {
+            if (sbytes)
                 asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(staged + e0),
                              "r"(in0 + buf * kPartTile * 8), "r"(sbytes)
                              : "memory");
-                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            }
+            // one group per tile, empty or not, so that "all groups but the
+            // newest" below always means the stores of tiles before this one
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
             // the last partial 16 bytes
             unsigned char* dst = reinterpret_cast<unsigned char*>(staged + e0);
             const unsigned char* srcb = reinterpret_cast<const unsigned char*>(in);
             for (unsigned bb = sbytes; bb < all; bb += 4)
                 *reinterpret_cast<unsigned*>(dst + bb) = *reinterpret_cast<const unsigned*>(srcb + bb);
+            // tile i + 2 into the buffer of tile i - 1, whose store has read it
+            const int64_t ahead = tile + (int64_t)(kPartBufs - 1) * gridDim.x;
+            if (ahead < ntiles) {
+                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(ahead, (int)((it + kPartBufs - 1) % kPartBufs));
+            }
         }
         // run bounds; bit 15 marks a tile staged as 4-byte records
         if (threadIdx.x <= P)
             bounds[tile * (P + 1) + threadIdx.x] = (unsigned short)(rstart[threadIdx.x] | (wide ? 0u : 0x8000u));
     }
     if (timed_out && threadIdx.x == 0) {
-        // let the loads in flight land before the shared memory is released
-        for (int q = 0; q < kPartBufs; ++q)
+        // let the loads in flight (tiles i and i + 1) land before the shared
+        // memory is released
+        for (int q = 0; q < kPartBufs - 1; ++q)
             if (tile + (int64_t)q * gridDim.x < ntiles)
                 mbar_wait_bounded(bar0 + 8 * ((it + q) % kPartBufs), ((it + q) / kPartBufs) & 1u);
         raise_error(err, ERRBIT_TIMEOUT);
