@@ -21,6 +21,7 @@
 //             above 2048 entries (64 rows x at most 256) go to an overflow list
 //             handled by a block-wide bitonic sort in 96 KB of shared memory.
 // Requires ncols < 2^24 (24-bit column field) and at most 256 entries per row.
+#include <climits>
 #include <cstring>
 #include <vector>
 
@@ -85,8 +86,19 @@ __global__ void __launch_bounds__(kBkThreads) bk_count_kernel(const BkInst* __re
         __syncthreads();
         const long long t0 = (long long)w.tile * kTileEntries;
         const long long t1 = t0 + kTileEntries < I.nnz ? t0 + kTileEntries : I.nnz;
-        for (long long k = t0 + threadIdx.x; k < t1; k += kBkThreads) {
-            const int r = I.rows[k];  // columns are checked by the split, which reads them anyway
+        // all of this thread's rows first (read-only loads, all in flight at
+        // once), then the counting: a load next to an atomic would otherwise
+        // wait for it, one memory round trip per entry
+        int rr[kTileEntries / kBkThreads];
+#pragma unroll
+        for (int j = 0; j < kTileEntries / kBkThreads; ++j) {
+            const long long k = t0 + threadIdx.x + (long long)j * kBkThreads;
+            rr[j] = k < t1 ? __ldg(I.rows + k) : INT_MIN;
+        }
+#pragma unroll
+        for (int j = 0; j < kTileEntries / kBkThreads; ++j) {
+            const int r = rr[j];  // columns are checked by the split, which reads them anyway
+            if (r == INT_MIN && t0 + threadIdx.x + (long long)j * kBkThreads >= t1) continue;
             if (r < 0 || r >= I.nrows) {
                 bad = true;
                 continue;
@@ -130,12 +142,20 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
         const long long t1 = t0 + kTileEntries < I.nnz ? t0 + kTileEntries : I.nnz;
         unsigned key[kSplitPer], rank[kSplitPer];
         int bucket[kSplitPer];
+        // the rows and columns of all this thread's entries first (read-only
+        // loads, all in flight at once), then the ranking atomics
 #pragma unroll
         for (int j = 0; j < kSplitPer; ++j) {
             const long long k = t0 + threadIdx.x + (long long)j * kBkThreads;
+            bucket[j] = k < t1 ? __ldg(I.rows + k) : -1;
+            key[j] = k < t1 ? (unsigned)__ldg(I.cols + k) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < kSplitPer; ++j) {
+            const long long k = t0 + threadIdx.x + (long long)j * kBkThreads;
+            const int r = bucket[j], c = (int)key[j];
             bucket[j] = -1;
             if (k < t1) {
-                const int r = I.rows[k], c = I.cols[k];
                 if (c < 0 || c >= I.ncols) bad = true;                 // (rows were checked by the count)
                 if (r >= 0 && r < I.nrows && c >= 0 && c < I.ncols) {
                     bucket[j] = r >> kBkShift;
@@ -164,17 +184,29 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
             }
         }
         __syncthreads();
+        // values in groups of four read-only loads, then their records
+        constexpr int kValGroup = 4;
 #pragma unroll
-        for (int j = 0; j < kSplitPer; ++j) {
-            if (bucket[j] < 0) continue;
-            const long long k = t0 + threadIdx.x + (long long)j * kBkThreads;
-            const long long pos = smem ? (long long)gbase[bucket[j]] + rank[j]
-                                       : bstart[I.bucket_base + bucket[j]] +
-                                             atomicAdd(&bfill[I.bucket_base + bucket[j]], 1u);
-            // one 16-byte record: the key, the entry's COO position (orders
-            // equal (row, col) keys) and the value
-            const double v = I.vals[k];
-            rec_out[pos] = make_uint4(key[j], (unsigned)k, (unsigned)__double2loint(v), (unsigned)__double2hiint(v));
+        for (int j0 = 0; j0 < kSplitPer; j0 += kValGroup) {
+            double v[kValGroup];
+#pragma unroll
+            for (int u = 0; u < kValGroup; ++u) {
+                const long long k = t0 + threadIdx.x + (long long)(j0 + u) * kBkThreads;
+                v[u] = bucket[j0 + u] >= 0 ? __ldg(I.vals + k) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kValGroup; ++u) {
+                const int j = j0 + u;
+                if (bucket[j] < 0) continue;
+                const long long k = t0 + threadIdx.x + (long long)j * kBkThreads;
+                const long long pos = smem ? (long long)gbase[bucket[j]] + rank[j]
+                                           : bstart[I.bucket_base + bucket[j]] +
+                                                 atomicAdd(&bfill[I.bucket_base + bucket[j]], 1u);
+                // one 16-byte record: the key, the entry's COO position (orders
+                // equal (row, col) keys) and the value
+                rec_out[pos] = make_uint4(key[j], (unsigned)k, (unsigned)__double2loint(v[u]),
+                                          (unsigned)__double2hiint(v[u]));
+            }
         }
         __syncthreads();
     }
