@@ -506,7 +506,8 @@ def suite_jacobi1d(hc, torch, peak, iters=100):
     return {"config": "jacobi_1d (a[i-1] + a[i] + a[i+1]) / 3.0 clamp, n=2^25 f64 U[0,1) seed 7, %d steps, CUDA graph"
                       % iters, "ms_per_step": round(ms, 4), "GB_s": round(gbs, 1),
             "frac_of_hbm_peak": round(gbs / peak, 3),
-            "note": "one IEEE division per point on GB300's FP64 unit (1.9 DFMA/clk/SM) bounds it"}
+            "note": "FP64-unit-bound on GB300 (1.9 DFMA/clk/SM): two sums on the integer pipe, the division by 3 "
+                    "as one multiply and two FMAs (bit-identical to IEEE division)"}
 
 
 def suite_gray_scott(hc, torch, peak, steps=5000):

@@ -61,4 +61,32 @@ __device__ __forceinline__ double dadd_pos(double x, double y) {
     return __longlong_as_double((long long)(((unsigned long long)e << 52) + (mant - kH)));
 }
 
+// ddiv_small_rn<D>(x) = x / D rounded to nearest even, for D = 3 or 5, in one
+// multiply and two FMAs instead of a full IEEE division (the published
+// correction scheme for division by a constant: Markstein, IBM J. R&D 1990;
+// Brisebarre, Muller, Raina, IEEE Trans. Computers 53(8), 2004):
+//   q0 = RN(x * z)            z = RN(1/D)
+//   r  = x - D * q0           exact (one FMA): |r| <= D/2 ulp(q0) plus a hair,
+//                             a multiple of ulp(q0) well inside 53 bits
+//   q  = RN(q0 + r * z)       one FMA
+// Why q is RN(x / D) for every finite x: q0 + r/D equals x/D exactly, and
+// replacing 1/D by z moves the FMA's exact argument by |r| * |z - 1/D|, under
+// 2^-54 ulp(q0).  x/D is either exact (then r = 0) or, since D is odd, lies k/D
+// of an ulp past a representable value (0 < k < D), at least 1/(2D) ulp away
+// from any rounding midpoint -- with subnormal results too, whose ulp is fixed.
+// A tiny shift cannot cross such a midpoint, so the single rounding of the FMA
+// gives the correctly rounded quotient.  A zero remainder (x/D exact, x = +-0
+// keeping its sign) and a non-finite q0 (x infinite or NaN) return q0 itself.
+template <int D>
+__device__ __forceinline__ double ddiv_small_rn(double x) {
+    static_assert(D == 3 || D == 5, "the correction is proved here for odd D = 3, 5");
+    constexpr double z = 1.0 / D;  // RN(1/D)
+    const double q0 = __dmul_rn(x, z);
+    const double r = __fma_rn(-(double)D, q0, x);
+    const unsigned long long qb = (unsigned long long)__double_as_longlong(q0);
+    const unsigned long long rb = (unsigned long long)__double_as_longlong(r);
+    if (((qb >> 52) & 0x7FFULL) == 0x7FFULL || (rb << 1) == 0ULL) return q0;
+    return __fma_rn(r, z, q0);
+}
+
 }  // namespace hyd

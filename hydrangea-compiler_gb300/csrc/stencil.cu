@@ -59,7 +59,7 @@ __device__ __forceinline__ double stencil_body(double a, double b, double c, dou
         const double lap = __fma_rn(-4.0, e, t3);
         return __dadd_rn(e, __dmul_rn(0.1, lap));
     }
-    return __ddiv_rn(__dadd_rn(t3, e), 5.0);
+    return ddiv_small_rn<5>(__dadd_rn(t3, e));  // = __ddiv_rn(., 5.0), bit for bit
 }
 
 // ---------------------------------------------------------------- plain path
@@ -457,6 +457,27 @@ __global__ void dadd_selftest_kernel(const double* __restrict__ x, const double*
     }
 }
 }  // namespace hyd
+
+__global__ void div_selftest_kernel(const double* __restrict__ x, int divisor, double* __restrict__ fast,
+                                    double* __restrict__ hw, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        fast[i] = divisor == 3 ? ddiv_small_rn<3>(x[i]) : ddiv_small_rn<5>(x[i]);
+        hw[i] = __ddiv_rn(x[i], (double)divisor);
+    }
+}
+
+extern "C" int hyd_cuda_selftest_div(const double* x, int divisor, double* fast, double* hw, int64_t n,
+                                     void* stream) {
+    HYD_CHECK_ARG(n >= 0 && (n == 0 || (x && fast && hw)), "selftest_div: bad arguments");
+    HYD_CHECK_ARG(divisor == 3 || divisor == 5, "selftest_div: divisor must be 3 or 5 (got %d)", divisor);
+    if (n == 0) return HYD_CUDA_OK;
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    const int64_t want = (n + 255) / 256;
+    const unsigned grid = (unsigned)(want < (int64_t)d->sm_count * 8 ? want : (int64_t)d->sm_count * 8);
+    div_selftest_kernel<<<grid, 256, 0, as_stream(stream)>>>(x, divisor, fast, hw, n);
+    return launch_check("selftest_div");
+}
 
 extern "C" int hyd_cuda_selftest_dadd(const double* x, const double* y, double* emu, double* hw, int64_t n,
                                       void* stream) {

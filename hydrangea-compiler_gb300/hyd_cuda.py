@@ -51,6 +51,7 @@ SIGNATURES = {
     "hyd_cuda_stencil_release_graphs": (None, []),
     "hyd_cuda_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i, _p]),
     "hyd_cuda_selftest_dadd": (_i, [_p, _p, _p, _p, _i64, _p]),
+    "hyd_cuda_selftest_div": (_i, [_p, _i, _p, _p, _i64, _p]),
     "hyd_cuda_iterate_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i64, _i, C.POINTER(C.c_int), _p]),
     "hyd_cuda_tune_cache_path": (C.c_char_p, []),
     "hyd_cuda_tune_set_cache_path": (_i, [C.c_char_p]),
@@ -322,6 +323,15 @@ def selftest_dadd(x, y):
     emu, hw = torch.empty_like(x), torch.empty_like(x)
     call("hyd_cuda_selftest_dadd", ptr(x), ptr(y), ptr(emu), ptr(hw), x.numel(), None)
     return emu, hw
+
+
+def selftest_div(x, divisor):
+    """(the multiply-and-two-FMA quotient, the IEEE quotient) of x / divisor,
+    divisor 3 or 5, both computed on the device."""
+    import torch
+    fast, hw = torch.empty_like(x), torch.empty_like(x)
+    call("hyd_cuda_selftest_div", ptr(x), divisor, ptr(fast), ptr(hw), x.numel(), None)
+    return fast, hw
 
 
 def autotune_stencil2d(kind, h, w, reps=5):

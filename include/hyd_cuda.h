@@ -168,6 +168,11 @@ int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t
  * unit's x[i] + y[i] (round to nearest even).  No counterpart in the
  * reference; for tests. */
 int hyd_cuda_selftest_dadd(const double* x, const double* y, double* emu, double* hw, int64_t n, void* stream);
+/* Self-test of the multiply-and-two-FMA division by 3 or 5 that jacobi_1d and
+ * the heat example's 5-point mean use: fast[i] = that quotient x[i] / divisor,
+ * hw[i] = the IEEE division (round to nearest even).  No counterpart in the
+ * reference; for tests. */
+int hyd_cuda_selftest_div(const double* x, int divisor, double* fast, double* hw, int64_t n, void* stream);
 /* ---- fused map / zipwith / generate chains -------------------------------------
  * The element loop of a fused chain (bench/map_chain/map_chain.hyd; the C
  * backend's loop body, CodegenC.hs:1328-1353 for the reduced form) with its

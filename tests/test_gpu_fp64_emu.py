@@ -66,3 +66,26 @@ def test_other_operand_classes_fall_back(hc, dev):
     xt, yt = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
     emu, hw = hc.selftest_dadd(xt, yt)
     assert np.array_equal(_bits(emu), _bits(hw))  # NaN payloads included: same FP64 unit
+
+
+@pytest.mark.parametrize("divisor", [3, 5])
+def test_small_division_correctly_rounded(hc, dev, divisor):
+    # the multiply-and-two-FMA quotient must equal IEEE division bit for bit:
+    # every exponent of both signs, subnormal inputs and results, exact
+    # quotients, signed zeros, the largest finite values, infinities, NaN
+    rng = np.random.default_rng(40 + divisor)
+    n = 1 << 21
+    x = _from_parts(rng, n, 0, 2046)
+    x[::2] = -x[::2]
+    k = rng.integers(1, 1 << 50, 1 << 16).astype(np.float64)
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, np.finfo(np.float64).max, -np.finfo(np.float64).max,
+                        np.finfo(np.float64).tiny, 5e-324, -5e-324, 1e-323, 2e-323, 1.0, 3.0, 5.0, 15.0, 1.5,
+                        2.0 ** -1022 * 3, 2.0 ** 1023, 0.1, 1.0 / 3.0])
+    x = np.concatenate([x, k * divisor, k * divisor + 1, (k * divisor) * 2.0 ** -1074, special])
+    fast, hw = hc.selftest_div(torch.from_numpy(x).to(dev), divisor)
+    fb, hb = _bits(fast), _bits(hw)
+    nan = np.isnan(x)
+    assert np.array_equal(fb[~nan], hb[~nan])
+    assert np.all(np.isnan(fast.cpu().numpy()[nan]))
+    ref = x / float(divisor)
+    assert np.array_equal(hb[~nan], ref.view(np.uint64)[~nan])
