@@ -55,6 +55,9 @@ static int64_t shape_size(const hyd_tuple_t& s) {
     return n;
 }
 
+// resident.cu: the device copy of an attached array (nullptr if not attached)
+int resident_device_data(const hyd_array_t* a, const void** out);
+
 [[noreturn]] static void export_fail(const char* what, int status) {
     // Keeps the reference runtime's failure behaviour for exported symbols:
     // message on stderr, exit(1) (runtime/hydrangea_runtime.h:322-328).
@@ -167,8 +170,31 @@ hyd_array_t* hyd_export_weighted_histogram(hyd_array_t* data, int64_t bins) {
     shape.elems[0] = bins;
     hyd_array_t* out = host_array_alloc(shape, 8);
     if (!out) export_fail("hyd_export_weighted_histogram", HYD_CUDA_ERR_NOMEM);
-    int s = hyd_cuda_weighted_histogram_host((const int64_t*)data->data, shape_size(data->shape), bins,
-                                             (int64_t*)out->data, HYD_SCATTER_AUTO);
+    const int64_t n = shape_size(data->shape);
+    const void* ddata = nullptr;
+    int s = resident_device_data(data, &ddata);
+    if (s == HYD_CUDA_OK && ddata) {
+        // an attached array: its device copy, no host->device traffic
+        Device* d = nullptr;
+        cudaStream_t st[2];
+        void* dh = nullptr;
+        s = device(&d);
+        if (s == HYD_CUDA_OK) s = side_streams(d, st);
+        if (s == HYD_CUDA_OK) s = device_buffer(d, "whist_bins", (size_t)bins * 8, &dh);
+        if (s == HYD_CUDA_OK && cudaMemsetAsync(dh, 0, (size_t)bins * 8, st[0]) != cudaSuccess)
+            s = set_error(HYD_CUDA_ERR_CUDA, "weighted_histogram: clearing the bins failed");
+        if (s == HYD_CUDA_OK)
+            s = hyd_cuda_weighted_histogram_i64((const int64_t*)ddata, n, bins, (int64_t*)dh, HYD_SCATTER_AUTO, st[0]);
+        if (s == HYD_CUDA_OK && cudaMemcpyAsync(out->data, dh, (size_t)bins * 8, cudaMemcpyDeviceToHost, st[0]) !=
+                                    cudaSuccess)
+            s = set_error(HYD_CUDA_ERR_CUDA, "weighted_histogram: reading the bins back failed");
+        if (s == HYD_CUDA_OK && cudaStreamSynchronize(st[0]) != cudaSuccess)
+            s = set_error(HYD_CUDA_ERR_CUDA, "weighted_histogram: synchronize failed");
+        if (s == HYD_CUDA_OK) s = hyd_cuda_check(st[0]);
+    } else if (s == HYD_CUDA_OK) {
+        s = hyd_cuda_weighted_histogram_host((const int64_t*)data->data, n, bins, (int64_t*)out->data,
+                                             HYD_SCATTER_AUTO);
+    }
     if (s != HYD_CUDA_OK) export_fail("hyd_export_weighted_histogram", s);
     return out;
 }
@@ -181,8 +207,28 @@ double hyd_export_dot(hyd_array_t* xs, hyd_array_t* ys) {
         export_fail("hyd_export_dot", HYD_CUDA_ERR_INVALID);
     }
     double r = 0.0;
-    int s = hyd_cuda_dot_f64_host((const double*)xs->data, (const double*)ys->data,
-                                  shape_size(xs->shape), &r);
+    const int64_t n = shape_size(xs->shape);
+    const void* dx = nullptr;
+    const void* dy = nullptr;
+    int s = resident_device_data(xs, &dx);
+    if (s == HYD_CUDA_OK) s = resident_device_data(ys, &dy);
+    if (s == HYD_CUDA_OK && dx && dy) {
+        // both arrays attached: their device copies, no host->device traffic
+        Device* d = nullptr;
+        cudaStream_t st[2];
+        void* dout = nullptr;
+        s = device(&d);
+        if (s == HYD_CUDA_OK) s = side_streams(d, st);
+        if (s == HYD_CUDA_OK) s = device_buffer(d, "export_dot_out", 8, &dout);
+        if (s == HYD_CUDA_OK) s = hyd_cuda_dot_f64((const double*)dx, (const double*)dy, n, (double*)dout, st[0]);
+        if (s == HYD_CUDA_OK && cudaMemcpyAsync(&r, dout, 8, cudaMemcpyDeviceToHost, st[0]) != cudaSuccess)
+            s = set_error(HYD_CUDA_ERR_CUDA, "dot: reading the result back failed");
+        if (s == HYD_CUDA_OK && cudaStreamSynchronize(st[0]) != cudaSuccess)
+            s = set_error(HYD_CUDA_ERR_CUDA, "dot: synchronize failed");
+        if (s == HYD_CUDA_OK) s = hyd_cuda_check(st[0]);
+    } else if (s == HYD_CUDA_OK) {
+        s = hyd_cuda_dot_f64_host((const double*)xs->data, (const double*)ys->data, n, &r);
+    }
     if (s != HYD_CUDA_OK) export_fail("hyd_export_dot", s);
     return r;
 }

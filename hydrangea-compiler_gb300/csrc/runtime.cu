@@ -11,7 +11,9 @@
 #include "hyd_common.cuh"
 
 namespace hyd {
-void release_map_kernels();  // jit_map.cu
+void release_map_kernels();      // jit_map.cu
+void release_resident_arrays();  // resident.cu
+void release_export_memos();     // stencil_more.cu
 }
 
 namespace hyd {
@@ -195,6 +197,8 @@ extern "C" void hyd_cuda_stencil_release_graphs(void);
 void hyd_cuda_cleanup(void) {
     hyd_cuda_stencil_release_graphs();
     release_map_kernels();
+    release_resident_arrays();
+    release_export_memos();
     std::lock_guard<std::mutex> lock(g_devices_mu);
     int cur = 0;
     if (cudaGetDevice(&cur) != cudaSuccess) cur = 0;

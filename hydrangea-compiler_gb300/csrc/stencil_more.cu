@@ -214,10 +214,10 @@ int hyd_cuda_iterate_gray_scott_f64(double* u0, double* v0, double* u1, double* 
     });
 }
 
-// The demo's exported procedure (gray_scott.hyd:80, called by demo/gray_scott/main.cpp:85):
-// V after 5000 steps on the 256 x 256 grid, as a host array the caller frees
-// with hyd_array_free.  Failures keep the reference's behaviour (stderr, exit 1).
-hyd_array_t* hyd_export_gray_scott(void) {
+// The demo's procedure (gray_scott.hyd:80, called by demo/gray_scott/main.cpp:85):
+// V after 5000 steps on the 256 x 256 grid, computed into a fresh host array.
+// Failures keep the reference's behaviour (stderr, exit 1).
+static hyd_array_t* gray_scott_compute(void) {
     const int64_t h = 256, w = 256, steps = 5000;
     hyd_tuple_t shape;
     shape.ndims = 2;
@@ -272,4 +272,45 @@ hyd_array_t* hyd_export_gray_scott(void) {
     return out;
 }
 
+// Like every zero-argument array procedure of the reference's C backend
+// (CodegenC.hs:690-707, :812-833), the export is memoised: the first call
+// computes the array and keeps one reference to it; every call returns a view,
+// a new header over the same storage with its reference count raised, which
+// the caller frees with hyd_array_free (runtime/hydrangea_runtime.h:319-343).
+// hyd_cuda_cleanup drops the runtime's own reference.
+static std::mutex g_gs_memo_mu;
+static hyd_array_t* g_gs_memo = nullptr;
+
+hyd_array_t* hyd_export_gray_scott(void) {
+    std::lock_guard<std::mutex> lock(g_gs_memo_mu);
+    if (!g_gs_memo) g_gs_memo = gray_scott_compute();
+    hyd_array_t* view = (hyd_array_t*)malloc(sizeof(hyd_array_t));
+    if (!view) {
+        fprintf(stderr, "hydrangea(cuda): hyd_export_gray_scott: host allocation failed\n");
+        exit(1);
+    }
+    *view = *g_gs_memo;
+    view->data = g_gs_memo->storage->data;
+    g_gs_memo->storage->refcount += 1;
+    return view;
+}
+
 }  // extern "C"
+
+namespace hyd {
+
+// What hyd_array_free does to the runtime's reference of each memoised export.
+void release_export_memos() {
+    std::lock_guard<std::mutex> lock(g_gs_memo_mu);
+    if (!g_gs_memo) return;
+    hyd_array_storage_t* st = g_gs_memo->storage;
+    st->refcount -= 1;
+    if (st->refcount == 0) {
+        free(st->data);
+        free(st);
+    }
+    free(g_gs_memo);
+    g_gs_memo = nullptr;
+}
+
+}  // namespace hyd

@@ -90,6 +90,11 @@ SIGNATURES = {
     "hyd_export_weighted_histogram": (_p, [_p, _i64]),
     "hyd_export_dot": (_d, [_p, _p]),
     "hyd_export_gray_scott": (_p, []),
+    "hyd_cuda_array_attach": (_i, [_p]),
+    "hyd_cuda_array_host_modified": (_i, [_p]),
+    "hyd_cuda_array_detach": (_i, [_p]),
+    "hyd_cuda_array_device_data": (_p, [_p]),
+    "hyd_cuda_array_resident_stats": (_i, [_p, _p, _p]),
     "hyd_cuda_map_f64": (_i, [C.c_char_p, _p, _i, _i64, _p, _p, _p]),
     "hyd_cuda_jacobi1d_f64": (_i, [_p, _p, _i64, _p]),
     "hyd_cuda_iterate_jacobi1d_f64": (_i, [_p, _p, _i64, _i64, C.POINTER(C.c_int), _p]),
@@ -506,6 +511,14 @@ def plain_trace(reqs, arrivals, stream=None):
     call("hyd_cuda_plain_trace", C.addressof(arr), t.ctypes.data, n, lat.ctypes.data, st.ctypes.data, C.byref(el),
          stream_handle(stream))
     return lat, st, el.value
+
+
+def resident_stats():
+    """(attached arrays, uploads so far, resident bytes) of the export path's
+    device-resident array copies."""
+    e, u, b = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+    call("hyd_cuda_array_resident_stats", C.byref(e), C.byref(u), C.byref(b))
+    return e.value, u.value, b.value
 
 
 def make_array(np_array):

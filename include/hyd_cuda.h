@@ -429,9 +429,33 @@ hyd_array_t* hyd_cuda_array_alloc(hyd_tuple_t shape, size_t elem_size);
 hyd_array_t* hyd_export_weighted_histogram(hyd_array_t* data, int64_t bins);
 /* demo/gray_scott's procedure (gray_scott.hyd:80; demo/gray_scott/main.cpp:85
  * calls it): V after 5000 steps on the demo's 256 x 256 grid from its initial
- * fields. */
+ * fields.  Memoised like the reference's zero-argument array procedures
+ * (CodegenC.hs:812-833): computed on the first call; every call returns a view
+ * over the same storage (reference count raised), freed with hyd_array_free.
+ * hyd_cuda_cleanup drops the runtime's own reference. */
 hyd_array_t* hyd_export_gray_scott(void);
+/* The exports below read an input array from its device-resident copy when
+ * the array is attached (next section); otherwise they stream its host data. */
 double hyd_export_dot(hyd_array_t* xs, hyd_array_t* ys);
+
+/* ---- device-resident arrays for the export path ----------------------------
+ * The reference keeps arrays in host memory; its Metal export lifecycle keeps
+ * the zero-argument array bindings as persistent GPU buffers across calls
+ * (CodegenMSL.hs:1253-1300).  Here any host array can be made resident:
+ *   attach         uploads the array and keeps a device copy beside
+ *                  storage->data (valid until the host declares a write);
+ *   host_modified  the host changed the data: the next use uploads again;
+ *   device_data    the device copy (uploaded first if stale), NULL when the
+ *                  array is not attached;
+ *   detach         frees the copy; call it before hyd_array_free.
+ * A copy belongs to (storage, data pointer, byte size): a view of another
+ * extent is a separate array.  hyd_cuda_cleanup frees every copy.
+ * resident_stats: attached arrays, uploads so far, resident bytes. */
+int hyd_cuda_array_attach(hyd_array_t* a);
+int hyd_cuda_array_host_modified(hyd_array_t* a);
+int hyd_cuda_array_detach(hyd_array_t* a);
+const void* hyd_cuda_array_device_data(hyd_array_t* a);
+int hyd_cuda_array_resident_stats(int64_t* entries, int64_t* uploads, int64_t* bytes);
 
 #ifdef __cplusplus
 }

@@ -81,3 +81,72 @@ def test_runtime_array_alloc_is_zeroed_and_freeable(hc):
     vals = np.ctypeslib.as_array(C.cast(a.data, C.POINTER(C.c_int64)), shape=(15,))
     assert not vals.any()
     _array_free(hc, p)
+
+
+def test_gray_scott_export_is_memoised(hc):
+    # like the reference's zero-argument array procedures (CodegenC.hs:812-833):
+    # one computation, then views over the same storage with the reference
+    # count raised; hyd_array_free of a view leaves the others valid
+    L = hc.lib()
+    f = L.hyd_export_gray_scott
+    f.restype = C.POINTER(hc.Array)
+    f.argtypes = []
+    a, b = f(), f()
+    sa, sb = a.contents, b.contents
+    assert C.cast(sa.storage, C.c_void_p).value == C.cast(sb.storage, C.c_void_p).value
+    assert sa.data == sb.data and sa.shape.elems[0] == 256 and sb.shape.elems[1] == 256
+    rc = sa.storage.contents.refcount
+    assert rc >= 3  # the runtime's own reference and these two views
+    first = np.ctypeslib.as_array(C.cast(sa.data, C.POINTER(C.c_double)), shape=(256, 256)).copy()
+    _array_free(hc, a)
+    assert sb.storage.contents.refcount == rc - 1
+    again = np.ctypeslib.as_array(C.cast(sb.data, C.POINTER(C.c_double)), shape=(256, 256))
+    assert np.array_equal(first, again)
+    _array_free(hc, b)
+
+
+def test_resident_arrays_skip_the_upload(hc, orc):
+    L = hc.lib()
+    n = 100_000
+    rng = np.random.default_rng(24)
+    xs, ys = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    ax, ay = hc.make_array(xs), hc.make_array(ys)
+    dot = L.hyd_export_dot
+    dot.restype = C.c_double
+    dot.argtypes = [C.POINTER(hc.Array), C.POINTER(hc.Array)]
+    streamed = dot(C.byref(ax), C.byref(ay))  # not attached: the host data is streamed
+    e0, u0, b0 = hc.resident_stats()
+    hc.check(L.hyd_cuda_array_attach(C.byref(ax)))
+    hc.check(L.hyd_cuda_array_attach(C.byref(ay)))
+    assert hc.resident_stats() == (e0 + 2, u0 + 2, b0 + 16 * n)
+    assert L.hyd_cuda_array_device_data(C.byref(ax)) is not None
+    # two calls read the device copies: same bits as the streamed call, no upload
+    assert dot(C.byref(ax), C.byref(ay)) == streamed
+    assert dot(C.byref(ax), C.byref(ay)) == streamed
+    assert hc.resident_stats()[1] == u0 + 2
+    # a declared host write is uploaded once, at the next use (doubling is exact)
+    xs *= 2.0
+    hc.check(L.hyd_cuda_array_host_modified(C.byref(ax)))
+    assert dot(C.byref(ax), C.byref(ay)) == 2.0 * streamed
+    assert hc.resident_stats()[1] == u0 + 3
+    hc.check(L.hyd_cuda_array_detach(C.byref(ax)))
+    hc.check(L.hyd_cuda_array_detach(C.byref(ay)))
+    assert hc.resident_stats()[0] == e0
+    assert L.hyd_cuda_array_device_data(C.byref(ax)) is None
+    assert L.hyd_cuda_array_detach(C.byref(ax)) == hc.ERR_INVALID  # not attached any more
+    hc.lib().hyd_cuda_check(None)
+
+    # the histogram export through a resident array
+    data = orc.uniform_i64(300_001, 25, 1 << 20)
+    ad = hc.make_array(data)
+    hc.check(L.hyd_cuda_array_attach(C.byref(ad)))
+    fn = L.hyd_export_weighted_histogram
+    fn.restype = C.POINTER(hc.Array)
+    fn.argtypes = [C.POINTER(hc.Array), C.c_int64]
+    for bins in (64, 65536):
+        out = fn(C.byref(ad), bins)
+        got = np.ctypeslib.as_array(C.cast(out.contents.data, C.POINTER(C.c_int64)), shape=(bins,)).copy()
+        assert np.array_equal(got, orc.weighted_hist(data, bins))
+        _array_free(hc, out)
+    assert hc.resident_stats()[1] == u0 + 4  # one upload, at attach
+    hc.check(L.hyd_cuda_array_detach(C.byref(ad)))

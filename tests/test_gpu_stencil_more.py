@@ -100,8 +100,13 @@ def test_export_gray_scott_matches_program(hc, orc, dev):
     u, v = _demo_init()
     _, ref_v = orc.gray_scott(u, v, 5000)
     assert np.array_equal(_bits(got), _bits(ref_v))
+    # what the reference's hyd_array_free does: the export is memoised, so this
+    # drops one reference of the storage and frees the header
     libc = C.CDLL(None)
     libc.free.argtypes = [C.c_void_p]
-    libc.free(a.storage.contents.data)
-    libc.free(C.cast(a.storage, C.c_void_p))
+    st = a.storage.contents
+    st.refcount -= 1
+    if st.refcount == 0:
+        libc.free(st.data)
+        libc.free(C.cast(a.storage, C.c_void_p))
     libc.free(C.cast(out, C.c_void_p))
