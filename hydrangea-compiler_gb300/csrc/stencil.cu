@@ -331,14 +331,82 @@ static int maps_for(int variant, const double* p, int64_t h, int64_t w, CUtensor
     return make_map(map, p, h, w, kTiles[shape].tw + 4, kTiles[shape].th + 2);
 }
 
-// Cached executable graphs of whole `iterate` runs.
+// ---- other boundary conditions -----------------------------------------------
+// `stencil wrap`, `stencil mirror` and `stencil (constant c)` (Syntax.hs:416-426)
+// with the same 5-point kinds and arithmetic.  Per dimension the neighbour index
+// is the one genBnd1DVar computes (Lowering.hs:2762-2812); for the footprint's
+// offsets of +-1 its formulas reduce to
+//   wrap    -1 -> n - 1,  n -> 0;
+//   mirror  -1 -> 1,      n -> n - 2   (n >= 2: the reference divides by zero
+//                                       for n == 1, which the host refuses);
+// `constant` reads `fill` when the index is out of range (genBnd2D,
+// Lowering.hs:2842-2870).  Interior points read their neighbours directly.
+enum { BND_CLAMP = 0, BND_WRAP = 1, BND_MIRROR = 2, BND_CONST = 3 };
+
+template <int KIND, int BND>
+__global__ void __launch_bounds__(256) stencil_bnd_kernel(const double* __restrict__ in, double* __restrict__ out,
+                                                          int64_t h, int64_t w, double fill) {
+    const int64_t j = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
+    const int64_t i = (int64_t)blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (i >= h || j >= w) return;
+    const double e = in[i * w + j];
+    double a, b, c, d;
+    if (i > 0 && i + 1 < h && j > 0 && j + 1 < w) {
+        a = in[(i - 1) * w + j];
+        b = in[(i + 1) * w + j];
+        c = in[i * w + j - 1];
+        d = in[i * w + j + 1];
+    } else if (BND == BND_CONST) {
+        a = i > 0 ? in[(i - 1) * w + j] : fill;
+        b = i + 1 < h ? in[(i + 1) * w + j] : fill;
+        c = j > 0 ? in[i * w + j - 1] : fill;
+        d = j + 1 < w ? in[i * w + j + 1] : fill;
+    } else {
+        const int64_t im = i > 0 ? i - 1 : (BND == BND_WRAP ? h - 1 : 1);
+        const int64_t ip = i + 1 < h ? i + 1 : (BND == BND_WRAP ? 0 : h - 2);
+        const int64_t jm = j > 0 ? j - 1 : (BND == BND_WRAP ? w - 1 : 1);
+        const int64_t jp = j + 1 < w ? j + 1 : (BND == BND_WRAP ? 0 : w - 2);
+        a = in[im * w + j];
+        b = in[ip * w + j];
+        c = in[i * w + jm];
+        d = in[i * w + jp];
+    }
+    out[i * w + j] = stencil_body<KIND, 2>(a, b, c, d, e);
+}
+
+template <int KIND>
+static int launch_bnd_kind(int bnd, double fill, const double* in, double* out, int64_t h, int64_t w,
+                           cudaStream_t s) {
+    const dim3 grid((unsigned)((w + 31) / 32), (unsigned)((h + 7) / 8));
+    switch (bnd) {
+        case BND_WRAP: stencil_bnd_kernel<KIND, BND_WRAP><<<grid, 256, 0, s>>>(in, out, h, w, fill); break;
+        case BND_MIRROR: stencil_bnd_kernel<KIND, BND_MIRROR><<<grid, 256, 0, s>>>(in, out, h, w, fill); break;
+        default: stencil_bnd_kernel<KIND, BND_CONST><<<grid, 256, 0, s>>>(in, out, h, w, fill); break;
+    }
+    return launch_check("stencil2d_bnd");
+}
+
+static int launch_bnd(int kind, int bnd, double fill, const double* in, double* out, int64_t h, int64_t w,
+                      cudaStream_t s) {
+    switch (kind) {
+        case ST_LAPLACIAN: return launch_bnd_kind<ST_LAPLACIAN>(bnd, fill, in, out, h, w, s);
+        case ST_JACOBI: return launch_bnd_kind<ST_JACOBI>(bnd, fill, in, out, h, w, s);
+        case ST_HEAT: return launch_bnd_kind<ST_HEAT>(bnd, fill, in, out, h, w, s);
+        default: return launch_bnd_kind<ST_HEAT_EXAMPLE>(bnd, fill, in, out, h, w, s);
+    }
+}
+
+// Cached executable graphs of whole `iterate` runs (`fill`: the constant of a
+// `constant` boundary, baked into the captured launches).
 struct GraphKey {
     int kind;
     int64_t h, w, iters;
     const void *b0, *b1;
     cudaStream_t stream;
+    double fill;
     bool operator<(const GraphKey& o) const {
-        return std::tie(kind, h, w, iters, b0, b1, stream) < std::tie(o.kind, o.h, o.w, o.iters, o.b0, o.b1, o.stream);
+        return std::tie(kind, h, w, iters, b0, b1, stream, fill) <
+               std::tie(o.kind, o.h, o.w, o.iters, o.b0, o.b1, o.stream, o.fill);
     }
 };
 static std::mutex g_graph_mu;
@@ -393,7 +461,7 @@ extern "C" int hyd_cuda_iterate_stencil2d_f64_variant(int kind, double* buf0, do
             HYD_TRY(launch_step(kind, &maps[t & 1], bufs[t & 1], bufs[(t + 1) & 1], h, w, v, d, st));
         return HYD_CUDA_OK;
     }
-    GraphKey key{kind * 256 + v, h, w, iters, buf0, buf1, st};
+    GraphKey key{kind * 256 + v, h, w, iters, buf0, buf1, st, 0.0};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_graph_mu);
@@ -432,6 +500,83 @@ extern "C" int hyd_cuda_iterate_stencil2d_f64_variant(int kind, double* buf0, do
 extern "C" int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
                                               int64_t iters, int* final_buf, void* stream) {
     return hyd_cuda_iterate_stencil2d_f64_variant(kind, buf0, buf1, h, w, iters, -1, final_buf, stream);
+}
+
+static int check_bnd(int kind, int boundary, int64_t h, int64_t w, const char* what) {
+    HYD_CHECK_ARG(kind >= 0 && kind <= 3, "%s: unknown kind %d", what, kind);
+    HYD_CHECK_ARG(boundary >= HYD_BOUNDARY_CLAMP && boundary <= HYD_BOUNDARY_CONSTANT, "%s: unknown boundary %d",
+                  what, boundary);
+    HYD_CHECK_ARG(h >= 0 && w >= 0, "%s: negative shape", what);
+    HYD_CHECK_ARG(boundary != HYD_BOUNDARY_MIRROR || h * w == 0 || (h >= 2 && w >= 2),
+                  "%s: a mirror boundary needs every extent >= 2 (%lld x %lld; the reference divides by zero)",
+                  what, (long long)h, (long long)w);
+    return HYD_CUDA_OK;
+}
+
+extern "C" int hyd_cuda_stencil2d_bnd_f64(int kind, int boundary, double fill, const double* in, double* out,
+                                          int64_t h, int64_t w, void* stream) {
+    HYD_TRY(check_bnd(kind, boundary, h, w, "stencil2d_bnd"));
+    if (boundary == HYD_BOUNDARY_CLAMP) return hyd_cuda_stencil2d_f64(kind, in, out, h, w, stream);
+    HYD_CHECK_ARG(h * w == 0 || (in != nullptr && out != nullptr), "stencil2d_bnd: null buffer");
+    HYD_CHECK_ARG(in != out || h * w == 0, "stencil2d_bnd: input and output must differ");
+    if (h == 0 || w == 0) return HYD_CUDA_OK;
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    return launch_bnd(kind, boundary, fill, in, out, h, w, as_stream(stream));
+}
+
+extern "C" int hyd_cuda_iterate_stencil2d_bnd_f64(int kind, int boundary, double fill, double* buf0, double* buf1,
+                                                  int64_t h, int64_t w, int64_t iters, int* final_buf,
+                                                  void* stream) {
+    HYD_TRY(check_bnd(kind, boundary, h, w, "iterate_stencil2d_bnd"));
+    if (boundary == HYD_BOUNDARY_CLAMP)
+        return hyd_cuda_iterate_stencil2d_f64(kind, buf0, buf1, h, w, iters, final_buf, stream);
+    HYD_CHECK_ARG(iters >= 0 && final_buf != nullptr, "iterate_stencil2d_bnd: bad count or null final_buf");
+    HYD_CHECK_ARG(h * w == 0 || (buf0 != nullptr && buf1 != nullptr && buf0 != buf1),
+                  "iterate_stencil2d_bnd: need two distinct buffers");
+    *final_buf = (int)(iters & 1);
+    if (h == 0 || w == 0 || iters == 0) return HYD_CUDA_OK;
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    cudaStream_t st = as_stream(stream);
+    double* bufs[2] = {buf0, buf1};
+    if (st == nullptr || iters < 4) {
+        for (int64_t t = 0; t < iters; ++t)
+            HYD_TRY(launch_bnd(kind, boundary, fill, bufs[t & 1], bufs[(t + 1) & 1], h, w, st));
+        return HYD_CUDA_OK;
+    }
+    // keys of this form sit above the clamp path's kind * 256 + variant (< 256)
+    GraphKey key{1024 + kind * 4 + boundary, h, w, iters, buf0, buf1, st, fill};
+    cudaGraphExec_t exec = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_graph_mu);
+        auto it = g_graphs.find(key);
+        if (it != g_graphs.end()) exec = it->second;
+    }
+    if (!exec) {
+        cudaGraph_t graph = nullptr;
+        HYD_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int status = HYD_CUDA_OK;
+        for (int64_t t = 0; t < iters && status == HYD_CUDA_OK; ++t)
+            status = launch_bnd(kind, boundary, fill, bufs[t & 1], bufs[(t + 1) & 1], h, w, st);
+        cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (status != HYD_CUDA_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return status;
+        }
+        HYD_CUDA_TRY(ce);
+        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        HYD_CUDA_TRY(ie);
+        std::lock_guard<std::mutex> lock(g_graph_mu);
+        if (g_graphs.size() >= 64) {
+            for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
+            g_graphs.clear();
+        }
+        g_graphs[key] = exec;
+    }
+    HYD_CUDA_TRY(cudaGraphLaunch(exec, st));
+    return HYD_CUDA_OK;
 }
 
 namespace hyd {

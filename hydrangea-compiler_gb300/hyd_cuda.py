@@ -48,6 +48,9 @@ SIGNATURES = {
     "hyd_cuda_scatter_add_f64": (_i, [_p, _p, _i64, _p, _i64, _p]),
     "hyd_cuda_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _p]),
     "hyd_cuda_iterate_stencil2d_f64": (_i, [_i, _p, _p, _i64, _i64, _i64, C.POINTER(C.c_int), _p]),
+    "hyd_cuda_stencil2d_bnd_f64": (_i, [_i, _i, C.c_double, _p, _p, _i64, _i64, _p]),
+    "hyd_cuda_iterate_stencil2d_bnd_f64": (_i, [_i, _i, C.c_double, _p, _p, _i64, _i64, _i64, C.POINTER(C.c_int),
+                                               _p]),
     "hyd_cuda_stencil_release_graphs": (None, []),
     "hyd_cuda_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i, _p]),
     "hyd_cuda_selftest_dadd": (_i, [_p, _p, _p, _p, _i64, _p]),
@@ -266,6 +269,24 @@ def iterate_stencil2d(kind, buf0, buf1, iters, stream=None, variant=-1):
     h, w = buf0.shape
     fb = C.c_int(-1)
     call("hyd_cuda_iterate_stencil2d_f64_variant", kind, ptr(buf0), ptr(buf1), h, w, iters, variant,
+         C.byref(fb), stream_handle(stream))
+    return buf0 if fb.value == 0 else buf1
+
+
+BOUNDARY_CLAMP, BOUNDARY_WRAP, BOUNDARY_MIRROR, BOUNDARY_CONSTANT = 0, 1, 2, 3
+
+
+def stencil2d_bnd(kind, boundary, src, dst, fill=0.0, stream=None):
+    """One step of a 5-point kind under a boundary condition."""
+    h, w = src.shape
+    call("hyd_cuda_stencil2d_bnd_f64", kind, boundary, fill, ptr(src), ptr(dst), h, w, stream_handle(stream))
+
+
+def iterate_stencil2d_bnd(kind, boundary, buf0, buf1, iters, fill=0.0, stream=None):
+    """`iters` steps under a boundary condition; returns the buffer holding the result."""
+    h, w = buf0.shape
+    fb = C.c_int(-1)
+    call("hyd_cuda_iterate_stencil2d_bnd_f64", kind, boundary, fill, ptr(buf0), ptr(buf1), h, w, iters,
          C.byref(fb), stream_handle(stream))
     return buf0 if fb.value == 0 else buf1
 

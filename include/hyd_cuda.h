@@ -163,6 +163,17 @@ int hyd_cuda_stencil2d_f64(int kind, const double* in, double* out, int64_t h, i
  * iters, stream) and replayed on later calls. */
 int hyd_cuda_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
                                    int64_t iters, int* final_buf, void* stream);
+/* The same kinds under the other boundary conditions of `stencil`
+ * (Syntax.hs:416-426): the neighbour index per dimension as the reference's
+ * lowering computes it (Lowering.hs:2762-2870) -- wrap: periodic; mirror:
+ * reflected without repeating the edge (every extent must be >= 2: the
+ * reference divides by zero otherwise, HYD_CUDA_ERR_INVALID here); constant:
+ * `fill` outside the array.  HYD_BOUNDARY_CLAMP takes the functions above. */
+enum { HYD_BOUNDARY_CLAMP = 0, HYD_BOUNDARY_WRAP = 1, HYD_BOUNDARY_MIRROR = 2, HYD_BOUNDARY_CONSTANT = 3 };
+int hyd_cuda_stencil2d_bnd_f64(int kind, int boundary, double fill, const double* in, double* out, int64_t h,
+                               int64_t w, void* stream);
+int hyd_cuda_iterate_stencil2d_bnd_f64(int kind, int boundary, double fill, double* buf0, double* buf1, int64_t h,
+                                       int64_t w, int64_t iters, int* final_buf, void* stream);
 /* Self-test of the integer-pipe binary64 addition the stencil variants of
  * levels 1-2 use: emu[i] = that addition of x[i] and y[i], hw[i] = the FP64
  * unit's x[i] + y[i] (round to nearest even).  No counterpart in the

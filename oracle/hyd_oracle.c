@@ -376,6 +376,124 @@ int orc_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, i
     return cur == buf0 ? 0 : 1;
 }
 
+/* Boundary conditions of `stencil` (Syntax.hs:416-426): per dimension, the
+ * index an offset access reads, as genBnd1DVar computes it
+ * (Lowering.hs:2762-2812):
+ *   clamp   max(0, min(raw, n-1));
+ *   wrap    raw - (raw / n) * n with C's truncating division, plus n when
+ *           negative;
+ *   mirror  period = 2 (n-1); r = raw - (raw / period) * period, plus period
+ *           when negative; then period - r when r >= n (a fold-back that
+ *           does not repeat the edge).  The reference divides by zero when
+ *           n == 1; callers refuse that extent.
+ * `constant` keeps the raw index; the caller reads the default instead when
+ * it is out of range (in 2-D when either index is, genBnd2D
+ * Lowering.hs:2842-2870).                                                    */
+int64_t orc_bound_index(int64_t raw, int64_t n, int mode) {
+    if (mode == ORC_BND_CLAMP) {
+        int64_t bi = raw;
+        if (raw < 0) bi = 0;
+        if (bi >= n) bi = n - 1;
+        return bi;
+    }
+    if (mode == ORC_BND_WRAP) {
+        int64_t q = raw / n;
+        int64_t bi = raw - q * n;
+        if (bi < 0) bi = bi + n;
+        return bi;
+    }
+    if (mode == ORC_BND_MIRROR) {
+        int64_t period = 2 * (n - 1);
+        int64_t q = raw / period;
+        int64_t r = raw - q * period;
+        if (r < 0) r = r + period;
+        if (r >= n) r = period - r;
+        return r;
+    }
+    return raw;
+}
+
+static int orc_bound_ok(int mode, int64_t n) { return !(mode == ORC_BND_MIRROR && n < 2); }
+
+/* Sum of `acc d` over the offsets, int64, in offset order: the 1-D stencils
+ * of StencilSpec.hs (`acc (-1)`, `acc 1`, `acc (-1) + acc 0 + acc 1`, ...).
+ * Returns -1 for a mirror boundary on an extent of 1.                      */
+int orc_stencil1d_offsets_i64(const int64_t* in, int64_t* out, int64_t n, const int64_t* offs, int noff,
+                              int mode, int64_t fill) {
+    if (!orc_bound_ok(mode, n)) return -1;
+    for (int64_t i = 0; i < n; i++) {
+        int64_t acc = 0;
+        for (int k = 0; k < noff; k++) {
+            int64_t raw = i + offs[k];
+            int64_t v;
+            if (mode == ORC_BND_CONST) v = (raw >= 0 && raw < n) ? in[raw] : fill;
+            else v = in[orc_bound_index(raw, n, mode)];
+            acc = (int64_t)((uint64_t)acc + (uint64_t)v);
+        }
+        out[i] = acc;
+    }
+    return 0;
+}
+
+/* 2-D form: offsets as (d0, d1) pairs; dimensions bounded independently,
+ * `constant` reads the default when either index is out of range.           */
+int orc_stencil2d_offsets_i64(const int64_t* in, int64_t* out, int64_t h, int64_t w, const int64_t* offs,
+                              int noff, int mode, int64_t fill) {
+    if (!orc_bound_ok(mode, h) || !orc_bound_ok(mode, w)) return -1;
+    for (int64_t i = 0; i < h; i++)
+        for (int64_t j = 0; j < w; j++) {
+            int64_t acc = 0;
+            for (int k = 0; k < noff; k++) {
+                int64_t r0 = i + offs[2 * k], r1 = j + offs[2 * k + 1];
+                int64_t v;
+                if (mode == ORC_BND_CONST)
+                    v = (r0 >= 0 && r0 < h && r1 >= 0 && r1 < w) ? in[r0 * w + r1] : fill;
+                else
+                    v = in[orc_bound_index(r0, h, mode) * w + orc_bound_index(r1, w, mode)];
+                acc = (int64_t)((uint64_t)acc + (uint64_t)v);
+            }
+            out[i * w + j] = acc;
+        }
+    return 0;
+}
+
+/* The 5-point kinds of orc_stencil2d_f64 under any boundary condition: the
+ * same body and evaluation order, neighbours read through orc_bound_index
+ * (`constant`: `fill` out of range).  Returns -1 for a mirror boundary on an
+ * extent of 1.  With ORC_BND_CLAMP it equals orc_stencil2d_f64.             */
+int orc_stencil2d_bnd_f64(int kind, int mode, double fill, const double* in, double* out, int64_t h,
+                          int64_t w) {
+    if (!orc_bound_ok(mode, h) || !orc_bound_ok(mode, w)) return -1;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int64_t i = 0; i < h; i++)
+        for (int64_t j = 0; j < w; j++) {
+            double nb[4];
+            const int64_t d0[4] = {-1, 1, 0, 0}, d1[4] = {0, 0, -1, 1};
+            for (int k = 0; k < 4; k++) {
+                int64_t r0 = i + d0[k], r1 = j + d1[k];
+                if (mode == ORC_BND_CONST)
+                    nb[k] = (r0 >= 0 && r0 < h && r1 >= 0 && r1 < w) ? in[r0 * w + r1] : fill;
+                else
+                    nb[k] = in[orc_bound_index(r0, h, mode) * w + orc_bound_index(r1, w, mode)];
+            }
+            out[i * w + j] = orc_stencil_body(kind, nb[0], nb[1], nb[2], nb[3], in[i * w + j]);
+        }
+    return 0;
+}
+
+int orc_iterate_stencil2d_bnd_f64(int kind, int mode, double fill, double* buf0, double* buf1, int64_t h,
+                                  int64_t w, int64_t iters) {
+    double* cur = buf0;
+    double* nxt = buf1;
+    for (int64_t t = 0; t < iters; t++) {
+        if (orc_stencil2d_bnd_f64(kind, mode, fill, cur, nxt, h, w) != 0) return -1;
+        double* tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    return cur == buf0 ? 0 : 1;
+}
+
 /* 1-D clamp 3-point box filter `acc (-1) + acc 0 + acc 1` (StencilSpec.hs:24-34). */
 void orc_stencil1d_box3_i64(const int64_t* in, int64_t* out, int64_t n) {
     for (int64_t i = 0; i < n; i++) {

@@ -49,6 +49,17 @@ void orc_stencil2d_f64(int kind, const double* in, double* out, int64_t h, int64
 int orc_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
                               int64_t iters);
 void orc_stencil1d_box3_i64(const int64_t* in, int64_t* out, int64_t n);
+/* boundary conditions (Syntax.hs:416-426; index arithmetic Lowering.hs:2762-2870) */
+enum { ORC_BND_CLAMP = 0, ORC_BND_WRAP = 1, ORC_BND_MIRROR = 2, ORC_BND_CONST = 3 };
+int64_t orc_bound_index(int64_t raw, int64_t n, int mode);
+int orc_stencil1d_offsets_i64(const int64_t* in, int64_t* out, int64_t n, const int64_t* offs, int noff,
+                              int mode, int64_t fill);
+int orc_stencil2d_offsets_i64(const int64_t* in, int64_t* out, int64_t h, int64_t w, const int64_t* offs,
+                              int noff, int mode, int64_t fill);
+int orc_stencil2d_bnd_f64(int kind, int mode, double fill, const double* in, double* out, int64_t h,
+                          int64_t w);
+int orc_iterate_stencil2d_bnd_f64(int kind, int mode, double fill, double* buf0, double* buf1, int64_t h,
+                                  int64_t w, int64_t iters);
 void orc_stencil1d_jacobi3_f64(const double* in, double* out, int64_t n);
 int orc_iterate_stencil1d_jacobi3_f64(double* buf0, double* buf1, int64_t n, int64_t iters);
 void orc_gray_scott_step_f64(const double* u, const double* v, double* un, double* vn, int64_t h, int64_t w,

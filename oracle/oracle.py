@@ -21,6 +21,8 @@ _i64 = C.c_int64
 _u64 = C.c_uint64
 
 LAPLACIAN, JACOBI, HEAT, HEAT_EXAMPLE = 0, 1, 2, 3
+# stencil boundary conditions (Syntax.hs:416-426)
+CLAMP, WRAP, MIRROR, CONST = 0, 1, 2, 3
 
 
 def lib():
@@ -45,6 +47,12 @@ def lib():
             "orc_stencil2d_f64": (None, [C.c_int, _f64p, _f64p, _i64, _i64]),
             "orc_iterate_stencil2d_f64": (C.c_int, [C.c_int, _f64p, _f64p, _i64, _i64, _i64]),
             "orc_stencil1d_box3_i64": (None, [_i64p, _i64p, _i64]),
+            "orc_bound_index": (_i64, [_i64, _i64, C.c_int]),
+            "orc_stencil1d_offsets_i64": (C.c_int, [_i64p, _i64p, _i64, _i64p, C.c_int, C.c_int, _i64]),
+            "orc_stencil2d_offsets_i64": (C.c_int, [_i64p, _i64p, _i64, _i64, _i64p, C.c_int, C.c_int, _i64]),
+            "orc_stencil2d_bnd_f64": (C.c_int, [C.c_int, C.c_int, C.c_double, _f64p, _f64p, _i64, _i64]),
+            "orc_iterate_stencil2d_bnd_f64": (C.c_int, [C.c_int, C.c_int, C.c_double, _f64p, _f64p, _i64, _i64,
+                                                        _i64]),
             "orc_stencil1d_jacobi3_f64": (None, [_f64p, _f64p, _i64]),
             "orc_iterate_stencil1d_jacobi3_f64": (C.c_int, [_f64p, _f64p, _i64, _i64]),
             "orc_gray_scott_step_f64": (None, [_f64p, _f64p, _f64p, _f64p, _i64, _i64, C.c_double, C.c_double,
@@ -159,6 +167,39 @@ def iterate_stencil2d(kind, grid, iters):
     b1 = np.empty_like(b0)
     h, w = b0.shape
     which = lib().orc_iterate_stencil2d_f64(kind, b0.reshape(-1), b1.reshape(-1), h, w, iters)
+    return b0 if which == 0 else b1
+
+
+def stencil1d_offsets(x, offsets, mode, fill=0):
+    """Sum of `acc d` over `offsets` under a boundary condition (int64)."""
+    x = np.ascontiguousarray(x, dtype=np.int64)
+    out = np.empty_like(x)
+    offs = np.ascontiguousarray(offsets, dtype=np.int64)
+    if lib().orc_stencil1d_offsets_i64(x, out, len(x), offs, len(offs), mode, fill) != 0:
+        raise ValueError("mirror boundary on an extent of 1")
+    return out
+
+
+def stencil2d_offsets(grid, offsets, mode, fill=0):
+    """2-D form; `offsets` is a list of (d0, d1) pairs."""
+    grid = np.ascontiguousarray(grid, dtype=np.int64)
+    h, w = grid.shape
+    out = np.empty_like(grid)
+    offs = np.ascontiguousarray(np.array(offsets, dtype=np.int64).reshape(-1))
+    if lib().orc_stencil2d_offsets_i64(grid.reshape(-1), out.reshape(-1), h, w, offs, len(offs) // 2, mode,
+                                        fill) != 0:
+        raise ValueError("mirror boundary on an extent of 1")
+    return out
+
+
+def stencil2d_bnd(kind, mode, grid, fill=0.0, iters=1):
+    """`iters` steps of a 5-point kind under a boundary condition."""
+    b0 = np.ascontiguousarray(grid, dtype=np.float64).copy()
+    b1 = np.empty_like(b0)
+    h, w = b0.shape
+    which = lib().orc_iterate_stencil2d_bnd_f64(kind, mode, fill, b0.reshape(-1), b1.reshape(-1), h, w, iters)
+    if which < 0:
+        raise ValueError("mirror boundary on an extent of 1")
     return b0 if which == 0 else b1
 
 

@@ -42,6 +42,32 @@ def known_answers():
         "source": "test/Language/Hydrangea/StencilSpec.hs:54-58",
         "input": [42], "expect": [126],
     }
+    # the boundary conditions of StencilSpec.hs: arrays, offsets, expected
+    # outputs (generate [4] (i + 1) is [1, 2, 3, 4])
+    ka["stencil_boundaries"] = {
+        "source": "test/Language/Hydrangea/StencilSpec.hs:37-148, :185-190",
+        "cases": [
+            {"line": 37, "mode": "clamp", "input": [0, 2, 4, 6], "offsets": [0], "expect": [0, 2, 4, 6]},
+            {"line": 43, "mode": "clamp", "input": [10, 11, 12], "offsets": [-5], "expect": [10, 10, 10]},
+            {"line": 50, "mode": "clamp", "input": [10, 11, 12], "offsets": [5], "expect": [12, 12, 12]},
+            {"line": 74, "mode": "wrap", "input": [1, 2, 3, 4], "offsets": [-1], "expect": [4, 1, 2, 3]},
+            {"line": 83, "mode": "wrap", "input": [1, 2, 3, 4], "offsets": [1], "expect": [2, 3, 4, 1]},
+            {"line": 91, "mode": "wrap", "input": [1, 2, 3, 4], "offsets": [-1, 0, 1], "expect_sum": 30},
+            {"line": 103, "mode": "mirror", "input": [1, 2, 3, 4], "offsets": [-1], "expect": [2, 1, 2, 3]},
+            {"line": 114, "mode": "mirror", "input": [1, 2, 3, 4], "offsets": [1], "expect": [2, 3, 4, 3]},
+            {"line": 126, "mode": "constant", "fill": 0, "input": [1, 2, 3], "offsets": [-1, 0, 1],
+             "expect": [3, 6, 5]},
+            {"line": 136, "mode": "constant", "fill": -1, "input": [10, 10, 10], "offsets": [-1],
+             "expect": [-1, 10, 10]},
+            {"line": 143, "mode": "constant", "fill": 99, "input": [0, 0], "offsets": [-5], "expect": [99, 99]},
+        ],
+        "cases2d": [
+            {"line": 161, "mode": "clamp", "input": [[1, 2, 3], [4, 5, 6]], "offsets": [[0, 1]],
+             "expect": [[2, 3, 3], [5, 6, 6]]},
+            {"line": 185, "mode": "constant", "fill": 0, "input": [[1, 1], [1, 1]], "offsets": [[-1, 0]],
+             "expect": [[0, 0], [1, 1]]},
+        ],
+    }
     ka["stencil2d_clamp_corner"] = {
         "source": "test/Language/Hydrangea/StencilSpec.hs:171-179",
         "input": [[1, 2, 3], [4, 5, 6], [7, 8, 9]], "index": [0, 0], "expect_sum4": 8,

@@ -107,3 +107,45 @@ def test_invalid_arguments(hc, dev):
     g = _grid(hc, 4, 4, dev)
     assert hc.lib().hyd_cuda_stencil2d_f64(7, g.data_ptr(), g.data_ptr(), 4, 4, None) == hc.ERR_INVALID
     assert hc.lib().hyd_cuda_stencil2d_f64(0, g.data_ptr(), g.data_ptr(), 4, 4, None) == hc.ERR_INVALID
+
+
+@pytest.mark.parametrize("boundary", ["wrap", "mirror", "constant"])
+@pytest.mark.parametrize("h,w", [(2, 2), (3, 7), (9, 1), (1, 6), (33, 65), (257, 130)])
+def test_other_boundaries_bit_exact(hc, orc, dev, boundary, h, w):
+    # stencil wrap / mirror / (constant c): every kind, one step and a captured
+    # 12-step iterate, bit for bit against the oracle's restatement of the
+    # reference's index arithmetic; mirror on an extent of 1 is refused
+    bmap = {"wrap": (hc.BOUNDARY_WRAP, orc.WRAP), "mirror": (hc.BOUNDARY_MIRROR, orc.MIRROR),
+            "constant": (hc.BOUNDARY_CONSTANT, orc.CONST)}
+    hb, ob = bmap[boundary]
+    fill = -0.75 if boundary == "constant" else 0.0
+    rng = np.random.default_rng(h * 1000 + w)
+    g = rng.uniform(-1, 1, (h, w))
+    src = torch.from_numpy(g).to(dev)
+    dst = torch.empty_like(src)
+    for kind in (hc.STENCIL_LAPLACIAN, hc.STENCIL_JACOBI, hc.STENCIL_HEAT, hc.STENCIL_HEAT_EXAMPLE):
+        if boundary == "mirror" and min(h, w) < 2:
+            with pytest.raises(hc.HydCudaError) as e:
+                hc.stencil2d_bnd(kind, hb, src, dst, fill)
+            assert e.value.status == hc.ERR_INVALID
+            continue
+        hc.stencil2d_bnd(kind, hb, src, dst, fill)
+        torch.cuda.synchronize()
+        ref = orc.stencil2d_bnd(kind, ob, g, fill)
+        assert np.array_equal(dst.cpu().numpy().view(np.uint64), ref.view(np.uint64)), kind
+        b0, b1 = src.clone(), torch.empty_like(src)
+        side = torch.cuda.Stream()
+        with torch.cuda.stream(side):
+            res = hc.iterate_stencil2d_bnd(kind, hb, b0, b1, 12, fill, stream=side)
+        side.synchronize()
+        ref = orc.stencil2d_bnd(kind, ob, g, fill, iters=12)
+        assert np.array_equal(res.cpu().numpy().view(np.uint64), ref.view(np.uint64)), kind
+
+
+def test_clamp_boundary_takes_the_tuned_path(hc, orc, dev):
+    g = np.random.default_rng(3).uniform(-1, 1, (40, 50))
+    src = torch.from_numpy(g).to(dev)
+    a, b = torch.empty_like(src), torch.empty_like(src)
+    hc.stencil2d_bnd(hc.STENCIL_LAPLACIAN, hc.BOUNDARY_CLAMP, src, a)
+    hc.stencil2d(hc.STENCIL_LAPLACIAN, src, b)
+    assert torch.equal(a, b)

@@ -259,3 +259,42 @@ def test_gray_scott_fixed_point(orc):
     import numpy as np
     u, v = orc.gray_scott(np.ones((9, 7)), np.zeros((9, 7)), 10)
     assert (u == 1.0).all() and (v == 0.0).all()
+
+
+def test_stencil_boundaries_known(orc, ka):
+    # StencilSpec.hs's clamp / wrap / mirror / constant cases, through the
+    # oracle's restatement of the reference's index arithmetic
+    modes = {"clamp": orc.CLAMP, "wrap": orc.WRAP, "mirror": orc.MIRROR, "constant": orc.CONST}
+    c = ka["stencil_boundaries"]
+    for case in c["cases"]:
+        out = orc.stencil1d_offsets(case["input"], case["offsets"], modes[case["mode"]], case.get("fill", 0))
+        if "expect" in case:
+            assert out.tolist() == case["expect"], case["line"]
+        else:
+            assert int(out.sum()) == case["expect_sum"], case["line"]
+    for case in c["cases2d"]:
+        out = orc.stencil2d_offsets(case["input"], case["offsets"], modes[case["mode"]], case.get("fill", 0))
+        assert out.tolist() == case["expect"], case["line"]
+
+
+def test_stencil_boundary_forms_agree(orc):
+    # the 5-point kinds under `clamp` equal the pinned clamp path; `wrap` and
+    # `mirror` read the neighbours the index arithmetic names; mirror on an
+    # extent of 1 is refused (the reference divides by zero there)
+    rng = np.random.default_rng(17)
+    for h, w in ((1, 1), (1, 7), (6, 1), (2, 2), (5, 9)):
+        g = rng.uniform(-1, 1, (h, w))
+        for kind in (orc.LAPLACIAN, orc.JACOBI, orc.HEAT, orc.HEAT_EXAMPLE):
+            assert np.array_equal(orc.stencil2d_bnd(kind, orc.CLAMP, g), orc.stencil2d(kind, g))
+    g = np.arange(12, dtype=np.float64).reshape(3, 4)
+    lap = orc.stencil2d_bnd(orc.LAPLACIAN, orc.WRAP, g)
+    # wrap at (0, 0): up = row 2, left = column 3
+    assert lap[0, 0] == g[2, 0] + g[1, 0] + g[0, 3] + g[0, 1] - 4 * g[0, 0]
+    lap = orc.stencil2d_bnd(orc.LAPLACIAN, orc.MIRROR, g)
+    assert lap[0, 0] == g[1, 0] + g[1, 0] + g[0, 1] + g[0, 1] - 4 * g[0, 0]
+    lap = orc.stencil2d_bnd(orc.LAPLACIAN, orc.CONST, g, fill=7.0)
+    assert lap[0, 0] == 7.0 + g[1, 0] + 7.0 + g[0, 1] - 4 * g[0, 0]
+    with pytest.raises(ValueError):
+        orc.stencil2d_bnd(orc.LAPLACIAN, orc.MIRROR, np.zeros((1, 5)))
+    assert [orc.lib().orc_bound_index(r, 4, orc.MIRROR) for r in range(-7, 11)] == \
+        [1, 0, 1, 2, 3, 2, 1, 0, 1, 2, 3, 2, 1, 0, 1, 2, 3, 2]
