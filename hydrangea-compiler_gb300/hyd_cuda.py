@@ -93,6 +93,14 @@ SIGNATURES = {
     "hyd_export_weighted_histogram": (_p, [_p, _i64]),
     "hyd_export_dot": (_d, [_p, _p]),
     "hyd_export_gray_scott": (_p, []),
+    "hyd_cuda_read_array_csv": (_p, [C.c_char_p, None]),
+    "hyd_cuda_read_float_array_csv": (_p, [C.c_char_p, None]),
+    "hyd_cuda_write_array_csv": (_i64, [_p, C.c_char_p]),
+    "hyd_cuda_write_array_csv_float": (_i64, [_p, C.c_char_p]),
+    "hyd_cuda_read_csv_i64_to_device": (_i, [C.c_char_p, _i64, _p, _p]),
+    "hyd_cuda_read_csv_f64_to_device": (_i, [C.c_char_p, _i64, _p, _p]),
+    "hyd_cuda_write_csv_i64_from_device": (_i, [_p, None, C.c_char_p, _p]),
+    "hyd_cuda_write_csv_f64_from_device": (_i, [_p, None, C.c_char_p, _p]),
     "hyd_cuda_array_attach": (_i, [_p]),
     "hyd_cuda_array_host_modified": (_i, [_p]),
     "hyd_cuda_array_detach": (_i, [_p]),

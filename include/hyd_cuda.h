@@ -449,6 +449,24 @@ hyd_array_t* hyd_export_gray_scott(void);
  * the array is attached (next section); otherwise they stream its host data. */
 double hyd_export_dot(hyd_array_t* xs, hyd_array_t* ys);
 
+/* ---- the host I/O path: CSV files ------------------------------------------
+ * Drop-in forms of the reference runtime's readers and writers
+ * (hyd_read_array_csv / hyd_read_float_array_csv,
+ * runtime/hydrangea_runtime.h:549-592; hyd_write_array_csv[_float],
+ * runtime/hyd_write_csv.c): the same grammar, values, output bytes and
+ * failures (a message on stderr, exit(1)), with the parsing and formatting
+ * spread over all host threads.  The *_to_device / *_from_device forms parse
+ * into pinned memory and copy to the device (or back) and return a status
+ * instead of exiting. */
+hyd_array_t* hyd_cuda_read_array_csv(const char* filename, hyd_tuple_t shape);
+hyd_array_t* hyd_cuda_read_float_array_csv(const char* filename, hyd_tuple_t shape);
+int64_t hyd_cuda_write_array_csv(hyd_array_t* arr, const char* filename);
+int64_t hyd_cuda_write_array_csv_float(hyd_array_t* arr, const char* filename);
+int hyd_cuda_read_csv_i64_to_device(const char* filename, int64_t n, int64_t* dev, void* stream);
+int hyd_cuda_read_csv_f64_to_device(const char* filename, int64_t n, double* dev, void* stream);
+int hyd_cuda_write_csv_i64_from_device(const int64_t* dev, hyd_tuple_t shape, const char* filename, void* stream);
+int hyd_cuda_write_csv_f64_from_device(const double* dev, hyd_tuple_t shape, const char* filename, void* stream);
+
 /* ---- device-resident arrays for the export path ----------------------------
  * The reference keeps arrays in host memory; its Metal export lifecycle keeps
  * the zero-argument array bindings as persistent GPU buffers across calls

@@ -95,6 +95,10 @@ def witness():
         W = C.CDLL(path)
         sig = {
             "wit_sort_indices": (None, [_i64p, _i64, _i64p]),
+            "wit_read_array_csv": (None, [C.c_char_p, _i64, _i64p]),
+            "wit_read_float_array_csv": (None, [C.c_char_p, _i64, _f64p]),
+            "wit_write_array_csv": (_i64, [_i64p, C.c_int, _i64, _i64, C.c_char_p]),
+            "wit_write_array_csv_float": (_i64, [_f64p, C.c_int, _i64, _i64, C.c_char_p]),
             "wit_nd_to_flat2": (_i64, [_i64, _i64, _i64, _i64]),
             "wit_whist": (None, [_i64, _i64, _i64p]),
             "wit_spmv": (None, [_i64, _i64, _i64, _f64p, _i64p, _i64p, _f64p, _f64p]),

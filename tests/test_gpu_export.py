@@ -150,3 +150,35 @@ def test_resident_arrays_skip_the_upload(hc, orc):
         _array_free(hc, out)
     assert hc.resident_stats()[1] == u0 + 4  # one upload, at attach
     hc.check(L.hyd_cuda_array_detach(C.byref(ad)))
+
+
+def test_csv_to_and_from_device(hc, tmp_path):
+    # the device forms of the host I/O path: what the host reader returns,
+    # copied to the device; what the host writer writes, read back from it;
+    # malformed input is a status, not an exit
+    import torch
+    L = hc.lib()
+    rng = np.random.default_rng(31)
+    ints = rng.integers(-(1 << 62), 1 << 62, 250_001)
+    flts = rng.standard_normal(250_001) * 1e-3
+    pi, pf = str(tmp_path / "i.csv"), str(tmp_path / "f.csv")
+    open(pi, "w").write(" ,".join(str(v) for v in ints) + "\n")
+    open(pf, "w").write("\n".join("%.17g" % v for v in flts))
+    di = torch.empty(len(ints), dtype=torch.int64, device="cuda")
+    df = torch.empty(len(flts), dtype=torch.float64, device="cuda")
+    hc.check(L.hyd_cuda_read_csv_i64_to_device(pi.encode(), len(ints), di.data_ptr(), None))
+    hc.check(L.hyd_cuda_read_csv_f64_to_device(pf.encode(), len(flts), df.data_ptr(), None))
+    assert np.array_equal(di.cpu().numpy(), ints)
+    assert np.array_equal(df.cpu().numpy().view(np.uint64), flts.view(np.uint64))
+    t = hc.Tuple()
+    t.ndims, t.elems[0], t.elems[1] = 2, 500, 500
+    oi, hi = str(tmp_path / "oi.csv"), str(tmp_path / "hi.csv")
+    hc.check(L.hyd_cuda_write_csv_i64_from_device(di.data_ptr(), t, oi.encode(), None))
+    block = np.ascontiguousarray(ints[:250_000].reshape(500, 500))
+    L.hyd_cuda_write_array_csv(C.byref(hc.make_array(block)), hi.encode())
+    assert open(oi, "rb").read() == open(hi, "rb").read()
+    bad = str(tmp_path / "bad.csv")
+    open(bad, "w").write("1,2,x")
+    assert L.hyd_cuda_read_csv_i64_to_device(bad.encode(), 3, di.data_ptr(), None) == hc.ERR_INVALID
+    assert L.hyd_cuda_read_csv_i64_to_device(str(tmp_path / "none.csv").encode(), 3, di.data_ptr(), None) == \
+        hc.ERR_INVALID
