@@ -120,6 +120,38 @@ struct ScatterI64Source {
     __device__ __forceinline__ u64 raw1(int64_t) const { return 0; }
 };
 
+// A scatter phase with a guard (Lowering.hs:1768-1790): element i takes part
+// only when guard[i] != 0.  Elements left out are routed to bin 0 with the
+// value 0, which leaves every sum unchanged, so their index is never checked
+// -- the reference does not read it either.
+struct GuardedScatterI64Source {
+    const int64_t* idx;
+    const int64_t* vals;
+    const int64_t* guard;
+    static constexpr bool kPackable = false;
+    static constexpr bool kMaskRoute = false;
+    __device__ __forceinline__ unsigned mask32() const { return 0u; }
+    __device__ __forceinline__ void one(int64_t i, long long& bin, u64& val) const {
+        const bool on = guard[i] != 0;
+        bin = on ? idx[i] : 0LL;
+        val = on ? (u64)vals[i] : 0ULL;
+    }
+    __device__ __forceinline__ bool four(int64_t v, long long bins, long long bin[4], u64 val[4]) const {
+        const u64x4 g = ldg_stream_u64x4(guard + 4 * v);
+        const u64x4 a = ldg_stream_u64x4(idx + 4 * v);
+        const u64x4 b = ldg_stream_u64x4(vals + 4 * v);
+        bin[0] = g.x ? (long long)a.x : 0LL; bin[1] = g.y ? (long long)a.y : 0LL;
+        bin[2] = g.z ? (long long)a.z : 0LL; bin[3] = g.w ? (long long)a.w : 0LL;
+        val[0] = g.x ? b.x : 0ULL; val[1] = g.y ? b.y : 0ULL; val[2] = g.z ? b.z : 0ULL; val[3] = g.w ? b.w : 0ULL;
+        return ((u64)bin[0] < (u64)bins) && ((u64)bin[1] < (u64)bins) && ((u64)bin[2] < (u64)bins) &&
+               ((u64)bin[3] < (u64)bins);
+    }
+    // unused (not packable)
+    __device__ __forceinline__ void route(u64, long long& bin, u64& val) const { bin = -1; val = 0; }
+    __device__ __forceinline__ u64x4 raw4(int64_t) const { return u64x4{0, 0, 0, 0}; }
+    __device__ __forceinline__ u64 raw1(int64_t) const { return 0; }
+};
+
 // Iterate this thread's elements: 32-byte groups t, t+S, ... (two in flight),
 // then the scalar remainder.  Groups whose routes are all in range go to
 // fast(bin, val) with no per-element check; everything else goes to
@@ -1240,6 +1272,25 @@ extern "C" int hyd_cuda_scatter_add_i64(const int64_t* idx, const int64_t* vals,
     bool vec = ((reinterpret_cast<uintptr_t>(idx) | reinterpret_cast<uintptr_t>(vals)) & 31) == 0;
     return hist_launch(src, n, vec, dst_n, reinterpret_cast<u64*>(dst), strategy, as_stream(stream),
                        "scatter_add_i64");
+}
+
+extern "C" int hyd_cuda_scatter_add_guarded_i64(const int64_t* idx, const int64_t* vals, const int64_t* guard,
+                                                int64_t n, int64_t* dst, int64_t dst_n, int strategy, void* stream) {
+    HYD_CHECK_ARG(n >= 0, "scatter_add_guarded_i64: negative length");
+    HYD_CHECK_ARG(dst_n > 0, "scatter_add_guarded_i64: empty destination");
+    HYD_CHECK_ARG(dst != nullptr, "scatter_add_guarded_i64: null destination");
+    HYD_CHECK_ARG(n == 0 || (idx != nullptr && vals != nullptr && guard != nullptr),
+                  "scatter_add_guarded_i64: null input");
+    HYD_CHECK_ARG(strategy >= HYD_SCATTER_AUTO && strategy <= HYD_SCATTER_PARTITION,
+                  "scatter_add_guarded_i64: unknown strategy %d", strategy);
+    HYD_CHECK_ARG(dst_n <= (1LL << 31), "scatter_add_guarded_i64: destination beyond 2^31 unsupported");
+    if (n == 0) return HYD_CUDA_OK;
+    GuardedScatterI64Source src{idx, vals, guard};
+    const bool vec =
+        ((reinterpret_cast<uintptr_t>(idx) | reinterpret_cast<uintptr_t>(vals) | reinterpret_cast<uintptr_t>(guard)) &
+         31) == 0;
+    return hist_launch(src, n, vec, dst_n, reinterpret_cast<u64*>(dst), strategy, as_stream(stream),
+                       "scatter_add_guarded_i64");
 }
 
 extern "C" int hyd_cuda_scatter_add_f64(const int64_t* idx, const double* vals, int64_t n,

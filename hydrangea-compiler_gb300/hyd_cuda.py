@@ -101,6 +101,9 @@ SIGNATURES = {
     "hyd_cuda_read_csv_f64_to_device": (_i, [C.c_char_p, _i64, _p, _p]),
     "hyd_cuda_write_csv_i64_from_device": (_i, [_p, None, C.c_char_p, _p]),
     "hyd_cuda_write_csv_f64_from_device": (_i, [_p, None, C.c_char_p, _p]),
+    "hyd_cuda_scatter_add_guarded_i64": (_i, [_p, _p, _p, _i64, _p, _i64, _i, _p]),
+    "hyd_cuda_reduce_rows_i64": (_i, [_p, _i64, _i64, _i, _i64, _p, _p]),
+    "hyd_cuda_reduce_rows_f64": (_i, [_p, _i64, _i64, _i, C.c_double, _p, _p]),
     "hyd_cuda_array_attach": (_i, [_p]),
     "hyd_cuda_array_host_modified": (_i, [_p]),
     "hyd_cuda_array_detach": (_i, [_p]),
@@ -282,6 +285,21 @@ def iterate_stencil2d(kind, buf0, buf1, iters, stream=None, variant=-1):
 
 
 BOUNDARY_CLAMP, BOUNDARY_WRAP, BOUNDARY_MIRROR, BOUNDARY_CONSTANT = 0, 1, 2, 3
+REDOP_ADD, REDOP_MUL = 0, 1
+
+
+def reduce_rows(x, op, init, out, stream=None):
+    """`reduce` over the trailing axis of a 2-D device tensor into `out` (rows,)."""
+    rows, cols = x.shape
+    if x.dtype.is_floating_point:
+        call("hyd_cuda_reduce_rows_f64", ptr(x), rows, cols, op, float(init), ptr(out), stream_handle(stream))
+    else:
+        call("hyd_cuda_reduce_rows_i64", ptr(x), rows, cols, op, int(init), ptr(out), stream_handle(stream))
+
+
+def scatter_add_guarded_i64(idx, vals, guard, dst, strategy=SCATTER_AUTO, stream=None):
+    call("hyd_cuda_scatter_add_guarded_i64", ptr(idx), ptr(vals), ptr(guard), idx.numel(), ptr(dst), dst.numel(),
+         strategy, stream_handle(stream))
 
 
 def stencil2d_bnd(kind, boundary, src, dst, fill=0.0, stream=None):

@@ -138,6 +138,23 @@ int hyd_cuda_scatter_add_i64(const int64_t* idx, const int64_t* vals, int64_t n,
                              int64_t* dst, int64_t dst_n, int strategy, void* stream);
 int hyd_cuda_scatter_add_f64(const int64_t* idx, const double* vals, int64_t n,
                              double* dst, int64_t dst_n, void* stream);
+/* A scatter (+) phase with a guard (Lowering.hs:1768-1790): element i takes
+ * part only when guard[i] != 0 (its index is not read otherwise).  Every
+ * strategy of the weighted histogram serves it; bit-exact. */
+int hyd_cuda_scatter_add_guarded_i64(const int64_t* idx, const int64_t* vals, const int64_t* guard, int64_t n,
+                                     int64_t* dst, int64_t dst_n, int strategy, void* stream);
+
+/* `reduce` over the trailing axis of an array [rows, cols] (EReduce,
+ * Lowering.hs:723-760): out[j] = init `op` x[j,0] `op` ... `op` x[j,cols-1],
+ * op one of the reference's reduction operators (CFGCore.hs:236).  int64
+ * wraps and is exact; f64 rows of up to 32 elements fold in the reference's
+ * order (bit-identical), longer ones by a fixed tree (deterministic, within
+ * rounding of the serial fold). */
+enum { HYD_REDOP_ADD = 0, HYD_REDOP_MUL = 1 };
+int hyd_cuda_reduce_rows_i64(const int64_t* in, int64_t rows, int64_t cols, int op, int64_t init, int64_t* out,
+                             void* stream);
+int hyd_cuda_reduce_rows_f64(const double* in, int64_t rows, int64_t cols, int op, double init, double* out,
+                             void* stream);
 
 /* ---- 2-D clamp stencils and iterate ---------------------------------------
  * Replaces the split-region clamp stencil loops (Lowering.hs:1932-2035,

@@ -494,6 +494,50 @@ int orc_iterate_stencil2d_bnd_f64(int kind, int mode, double fill, double* buf0,
     return cur == buf0 ? 0 : 1;
 }
 
+/* `reduce` over the trailing axis (EReduce, Lowering.hs:723-760): for each
+ * outer index j, acc = init; acc = acc op x[j*cols + k] for k in order;
+ * out[j] = acc.  op 0: (+), 1: (*) (the Redop set, CFGCore.hs:236).  int64
+ * arithmetic wraps.                                                          */
+void orc_reduce_rows_i64(const int64_t* in, int64_t rows, int64_t cols, int op, int64_t init, int64_t* out) {
+    for (int64_t j = 0; j < rows; j++) {
+        uint64_t acc = (uint64_t)init;
+        for (int64_t k = 0; k < cols; k++) {
+            uint64_t x = (uint64_t)in[j * cols + k];
+            acc = op == 0 ? acc + x : acc * x;
+        }
+        out[j] = (int64_t)acc;
+    }
+}
+
+void orc_reduce_rows_f64(const double* in, int64_t rows, int64_t cols, int op, double init, double* out) {
+    for (int64_t j = 0; j < rows; j++) {
+        double acc = init;
+        for (int64_t k = 0; k < cols; k++) {
+            double x = in[j * cols + k];
+            acc = op == 0 ? acc + x : acc * x;
+        }
+        out[j] = acc;
+    }
+}
+
+/* A scatter (+) phase with a guard over materialised arrays (EScatterChain,
+ * Lowering.hs:1768-1790): if guard[i] then dst[idx[i]] += vals[i].  Returns
+ * -1 when a guarded index is out of range (the reference does not check).   */
+int orc_scatter_add_guarded_i64(const int64_t* idx, const int64_t* vals, const int64_t* guard, int64_t n,
+                                int64_t* dst, int64_t dst_n) {
+    int bad = 0;
+    for (int64_t i = 0; i < n; i++) {
+        if (!guard[i]) continue;
+        int64_t b = idx[i];
+        if (b < 0 || b >= dst_n) {
+            bad = 1;
+            continue;
+        }
+        dst[b] = (int64_t)((uint64_t)dst[b] + (uint64_t)vals[i]);
+    }
+    return bad ? -1 : 0;
+}
+
 /* 1-D clamp 3-point box filter `acc (-1) + acc 0 + acc 1` (StencilSpec.hs:24-34). */
 void orc_stencil1d_box3_i64(const int64_t* in, int64_t* out, int64_t n) {
     for (int64_t i = 0; i < n; i++) {

@@ -49,6 +49,10 @@ void orc_stencil2d_f64(int kind, const double* in, double* out, int64_t h, int64
 int orc_iterate_stencil2d_f64(int kind, double* buf0, double* buf1, int64_t h, int64_t w,
                               int64_t iters);
 void orc_stencil1d_box3_i64(const int64_t* in, int64_t* out, int64_t n);
+void orc_reduce_rows_i64(const int64_t* in, int64_t rows, int64_t cols, int op, int64_t init, int64_t* out);
+void orc_reduce_rows_f64(const double* in, int64_t rows, int64_t cols, int op, double init, double* out);
+int orc_scatter_add_guarded_i64(const int64_t* idx, const int64_t* vals, const int64_t* guard, int64_t n,
+                                int64_t* dst, int64_t dst_n);
 /* boundary conditions (Syntax.hs:416-426; index arithmetic Lowering.hs:2762-2870) */
 enum { ORC_BND_CLAMP = 0, ORC_BND_WRAP = 1, ORC_BND_MIRROR = 2, ORC_BND_CONST = 3 };
 int64_t orc_bound_index(int64_t raw, int64_t n, int mode);

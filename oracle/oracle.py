@@ -48,6 +48,9 @@ def lib():
             "orc_iterate_stencil2d_f64": (C.c_int, [C.c_int, _f64p, _f64p, _i64, _i64, _i64]),
             "orc_stencil1d_box3_i64": (None, [_i64p, _i64p, _i64]),
             "orc_bound_index": (_i64, [_i64, _i64, C.c_int]),
+            "orc_reduce_rows_i64": (None, [_i64p, _i64, _i64, C.c_int, _i64, _i64p]),
+            "orc_reduce_rows_f64": (None, [_f64p, _i64, _i64, C.c_int, C.c_double, _f64p]),
+            "orc_scatter_add_guarded_i64": (C.c_int, [_i64p, _i64p, _i64p, _i64, _i64p, _i64]),
             "orc_stencil1d_offsets_i64": (C.c_int, [_i64p, _i64p, _i64, _i64p, C.c_int, C.c_int, _i64]),
             "orc_stencil2d_offsets_i64": (C.c_int, [_i64p, _i64p, _i64, _i64, _i64p, C.c_int, C.c_int, _i64]),
             "orc_stencil2d_bnd_f64": (C.c_int, [C.c_int, C.c_int, C.c_double, _f64p, _f64p, _i64, _i64]),
@@ -172,6 +175,27 @@ def iterate_stencil2d(kind, grid, iters):
     h, w = b0.shape
     which = lib().orc_iterate_stencil2d_f64(kind, b0.reshape(-1), b1.reshape(-1), h, w, iters)
     return b0 if which == 0 else b1
+
+
+def reduce_rows(x, op, init):
+    """`reduce` (op 0: +, 1: *) over the trailing axis of a 2-D array, serially."""
+    rows, cols = x.shape
+    if x.dtype == np.float64:
+        out = np.empty(rows, np.float64)
+        lib().orc_reduce_rows_f64(np.ascontiguousarray(x).reshape(-1), rows, cols, op, float(init), out)
+    else:
+        out = np.empty(rows, np.int64)
+        lib().orc_reduce_rows_i64(np.ascontiguousarray(x, dtype=np.int64).reshape(-1), rows, cols, op, int(init),
+                                  out)
+    return out
+
+
+def scatter_add_guarded_i64(idx, vals, guard, dst_n):
+    dst = np.zeros(dst_n, np.int64)
+    st = lib().orc_scatter_add_guarded_i64(np.ascontiguousarray(idx, dtype=np.int64),
+                                           np.ascontiguousarray(vals, dtype=np.int64),
+                                           np.ascontiguousarray(guard, dtype=np.int64), len(idx), dst, dst_n)
+    return dst, st
 
 
 def stencil1d_offsets(x, offsets, mode, fill=0):

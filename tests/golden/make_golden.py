@@ -68,6 +68,11 @@ def known_answers():
              "expect": [[0, 0], [1, 1]]},
         ],
     }
+    # reduce over the trailing axis of generate [2,3] (i*10 + j)
+    ka["reduce_trailing_axis_2d"] = {
+        "source": "test/Language/Hydrangea/InterpreterSpec.hs:337-342",
+        "input": [[0, 1, 2], [10, 11, 12]], "init": 0, "expect": [3, 33],
+    }
     ka["stencil2d_clamp_corner"] = {
         "source": "test/Language/Hydrangea/StencilSpec.hs:171-179",
         "input": [[1, 2, 3], [4, 5, 6], [7, 8, 9]], "index": [0, 0], "expect_sum4": 8,

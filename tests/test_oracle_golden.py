@@ -298,3 +298,22 @@ def test_stencil_boundary_forms_agree(orc):
         orc.stencil2d_bnd(orc.LAPLACIAN, orc.MIRROR, np.zeros((1, 5)))
     assert [orc.lib().orc_bound_index(r, 4, orc.MIRROR) for r in range(-7, 11)] == \
         [1, 0, 1, 2, 3, 2, 1, 0, 1, 2, 3, 2, 1, 0, 1, 2, 3, 2]
+
+
+def test_reduce_trailing_axis_known(orc, ka):
+    c = ka["reduce_trailing_axis_2d"]
+    x = np.array(c["input"], dtype=np.int64)
+    assert orc.reduce_rows(x, 0, c["init"]).tolist() == c["expect"]
+    # the same rows as floats, and (*) with a wrapping int64 product
+    assert orc.reduce_rows(x.astype(np.float64), 0, 0.0).tolist() == [3.0, 33.0]
+    big = np.array([[1 << 40, 1 << 40]], dtype=np.int64)
+    assert orc.reduce_rows(big, 1, 1).tolist() == [0]  # 2^80 wraps to 0
+
+
+def test_guarded_scatter_skips_unguarded_routes(orc):
+    # an unguarded element's index is not read: out of range there is fine
+    idx = np.array([0, 5, 1, -7, 1], np.int64)
+    vals = np.array([10, 20, 30, 40, 50], np.int64)
+    guard = np.array([1, 1, 1, 0, 2], np.int64)
+    dst, st = orc.scatter_add_guarded_i64(idx, vals, guard, 6)
+    assert st == 0 and dst.tolist() == [10, 80, 0, 0, 0, 20]
