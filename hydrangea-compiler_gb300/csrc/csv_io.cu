@@ -272,26 +272,6 @@ int64_t shape_elems(const hyd_tuple_t& s) {
     return n;
 }
 
-hyd_array_t* alloc_host_array(const hyd_tuple_t& shape, size_t elem) {
-    const int64_t n = shape_elems(shape);
-    hyd_array_storage_t* st = (hyd_array_storage_t*)malloc(sizeof(hyd_array_storage_t));
-    hyd_array_t* a = (hyd_array_t*)malloc(sizeof(hyd_array_t));
-    unsigned char* data = (unsigned char*)calloc((size_t)(n > 0 ? n : 1), elem);
-    if (!st || !a || !data) {
-        free(st);
-        free(a);
-        free(data);
-        return nullptr;
-    }
-    st->data = data;
-    st->refcount = 1;
-    a->storage = st;
-    a->data = data;
-    a->elem_size = elem;
-    a->shape = shape;
-    return a;
-}
-
 // The rows of the output, formatted on all host threads, in order.
 template <class T>
 std::string format_rows(const T* v, int ndims, const hyd_tuple_t& shape) {
@@ -350,7 +330,7 @@ hyd_array_t* read_host(const char* path, hyd_tuple_t shape, const char* who) {
         fprintf(stderr, "%s: cannot open '%s'\n", who, path);
         exit(1);
     }
-    hyd_array_t* a = alloc_host_array(shape, 8);
+    hyd_array_t* a = hyd_cuda_array_alloc(shape, 8);  // what the reference's hyd_array_free releases
     if (!a) {
         fprintf(stderr, "%s: out of memory\n", who);
         exit(1);
