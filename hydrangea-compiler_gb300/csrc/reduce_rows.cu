@@ -8,9 +8,12 @@
 //   * rows of up to 32 elements: one thread per row, folding in the
 //     reference's order -- bit-identical to it, floats included;
 //   * longer rows: a warp per row (or a 256-thread block when there are few
-//     rows), each lane folding the elements k = lane, lane + W, ... from the
-//     identity, then a fixed tree, then init combined last: deterministic, and
-//     within rounding of the serial fold for floats (integers wrap, exact).
+//     rows), each lane folding the elements k = lane, lane + W, ... into four
+//     interleaved accumulators from the identity, then a fixed tree, then init
+//     combined last: deterministic, and within rounding of the serial fold for
+//     floats (integers wrap, exact);
+//   * a few very long rows: each row split into chunks over many blocks, whose
+//     partials a second pass folds in chunk order.
 #include <type_traits>
 
 #include "hyd_common.cuh"
@@ -48,37 +51,64 @@ __device__ __forceinline__ T warp_tree(T v) {
     return v;
 }
 
+// this thread's fold of r[k0], r[k0 + W], ... below `end`: four interleaved
+// accumulators (loads in flight together), combined in a fixed order
+template <class T, int OP, int W>
+__device__ __forceinline__ T strided_fold(const T* __restrict__ r, int64_t k0, int64_t end) {
+    T a0 = ridentity<T, OP>(), a1 = a0, a2 = a0, a3 = a0;
+    int64_t k = k0;
+    for (; k + 3 * W < end; k += 4 * W) {
+        a0 = rcomb<T, OP>(a0, __ldg(r + k));
+        a1 = rcomb<T, OP>(a1, __ldg(r + k + W));
+        a2 = rcomb<T, OP>(a2, __ldg(r + k + 2 * W));
+        a3 = rcomb<T, OP>(a3, __ldg(r + k + 3 * W));
+    }
+    for (; k < end; k += W) a0 = rcomb<T, OP>(a0, __ldg(r + k));
+    return rcomb<T, OP>(rcomb<T, OP>(a0, a1), rcomb<T, OP>(a2, a3));
+}
+
 template <class T, int OP>
 __global__ void rows_warp_kernel(const T* __restrict__ in, int64_t rows, int64_t cols, T init, T* __restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t j = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < rows; j += warps) {
-        const T* r = in + j * cols;
-        T acc = ridentity<T, OP>();
-        for (int64_t k = lane; k < cols; k += 32) acc = rcomb<T, OP>(acc, __ldg(r + k));
-        acc = warp_tree<T, OP>(acc);
+        T acc = warp_tree<T, OP>(strided_fold<T, OP, 32>(in + j * cols, lane, cols));
         if (lane == 0) out[j] = rcomb<T, OP>(init, acc);
     }
 }
 
+// Block j % nchunks of row j / nchunks folds its chunk [c * chunk, ..) of
+// the row into part[j] (nchunks == 1: the whole row, then init, into out).
 template <class T, int OP>
-__global__ void __launch_bounds__(256) rows_block_kernel(const T* __restrict__ in, int64_t rows, int64_t cols, T init,
-                                                         T* __restrict__ out) {
-    __shared__ T part[8];
+__global__ void __launch_bounds__(256) rows_block_kernel(const T* __restrict__ in, int64_t rows, int64_t cols,
+                                                         int64_t nchunks, int64_t chunk, T init, T* __restrict__ out,
+                                                         T* __restrict__ part) {
+    __shared__ T wpart[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int64_t j = blockIdx.x; j < rows; j += gridDim.x) {
-        const T* r = in + j * cols;
-        T acc = ridentity<T, OP>();
-        for (int64_t k = threadIdx.x; k < cols; k += 256) acc = rcomb<T, OP>(acc, __ldg(r + k));
-        acc = warp_tree<T, OP>(acc);
-        if (lane == 0) part[warp] = acc;
+    for (int64_t j = blockIdx.x; j < rows * nchunks; j += gridDim.x) {
+        const int64_t row = j / nchunks, c = j % nchunks;
+        const int64_t lo = c * chunk, hi = lo + chunk < cols ? lo + chunk : cols;
+        T acc = warp_tree<T, OP>(strided_fold<T, OP, 256>(in + row * cols, lo + threadIdx.x, hi));
+        if (lane == 0) wpart[warp] = acc;
         __syncthreads();
         if (threadIdx.x == 0) {
-            T t = part[0];
-            for (int w = 1; w < 8; ++w) t = rcomb<T, OP>(t, part[w]);
-            out[j] = rcomb<T, OP>(init, t);
+            T t = wpart[0];
+            for (int w = 1; w < 8; ++w) t = rcomb<T, OP>(t, wpart[w]);
+            if (nchunks == 1) out[row] = rcomb<T, OP>(init, t);
+            else part[j] = t;
         }
         __syncthreads();
+    }
+}
+
+// init, then the chunks' partials of each row in chunk order
+template <class T, int OP>
+__global__ void rows_combine_kernel(const T* __restrict__ part, int64_t rows, int64_t nchunks, T init,
+                                    T* __restrict__ out) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < rows; j += (int64_t)gridDim.x * blockDim.x) {
+        T acc = init;
+        for (int64_t c = 0; c < nchunks; ++c) acc = rcomb<T, OP>(acc, part[j * nchunks + c]);
+        out[j] = acc;
     }
 }
 
@@ -94,7 +124,31 @@ static int launch_rows(const T* in, int64_t rows, int64_t cols, T init, T* out, 
         const int64_t want = (rows + 7) / 8;
         rows_warp_kernel<T, OP><<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(in, rows, cols, init, out);
     } else {
-        rows_block_kernel<T, OP><<<(unsigned)(rows < cap ? rows : cap), 256, 0, s>>>(in, rows, cols, init, out);
+        // enough blocks for the whole GPU: long rows split into chunks of at
+        // least 2^14 elements
+        int64_t nchunks = 1, chunk = cols;
+        const int64_t want_blocks = (int64_t)d->sm_count * 8;
+        if (rows < want_blocks && cols >= (int64_t)1 << 15) {
+            nchunks = (want_blocks + rows - 1) / rows;
+            const int64_t most = (cols + ((int64_t)1 << 14) - 1) >> 14;
+            if (nchunks > most) nchunks = most;
+            chunk = (cols + nchunks - 1) / nchunks;
+            nchunks = (cols + chunk - 1) / chunk;
+        }
+        T* part = nullptr;
+        if (nchunks > 1) {
+            unsigned* counters = nullptr;
+            void* scratch = nullptr;
+            HYD_TRY(workspace(s, (size_t)(rows * nchunks) * sizeof(T), &counters, &scratch));
+            part = static_cast<T*>(scratch);
+        }
+        const int64_t blocks = rows * nchunks;
+        rows_block_kernel<T, OP><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(in, rows, cols, nchunks,
+                                                                                         chunk, init, out, part);
+        if (nchunks > 1) {
+            HYD_TRY(launch_check("reduce_rows"));
+            rows_combine_kernel<T, OP><<<1, 256, 0, s>>>(part, rows, nchunks, init, out);
+        }
     }
     return launch_check("reduce_rows");
 }

@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("rows,cols", [(0, 5), (5, 0), (1, 1), (7, 3), (1000, 31), (1000, 32), (1000, 33),
-                                       (3, 100_003), (200_000, 50), (64, 4096), (3000, 700)])
+                                       (3, 100_003), (5, 1_000_003), (200_000, 50), (64, 4096), (3000, 700)])
 @pytest.mark.parametrize("op", [0, 1])
 def test_reduce_rows(hc, orc, dev, rows, cols, op):
     rng = np.random.default_rng(rows * 7 + cols + op)
