@@ -12,7 +12,8 @@ element per launch, plus the B*8 B histogram write).
 
 --impl reference times the C-backend restatement (the oracle port, OpenMP on
 all host cores) on the same configuration; under torchrun only rank 0 runs it.
-Other workloads of the suite run with --workload dot|heat|batched|serve.
+Other workloads of the suite run with --workload
+dot|map_zipwith|map_chain|heat|jacobi1d|gray_scott|scan|segreduce|batched|serve.
 """
 import argparse
 import json
@@ -41,7 +42,8 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="histogram",
-                   choices=["histogram", "dot", "map_chain", "heat", "jacobi1d", "gray_scott", "batched", "serve"],
+                   choices=["histogram", "dot", "map_zipwith", "map_chain", "heat", "jacobi1d", "gray_scott",
+                            "scan", "segreduce", "batched", "serve"],
                    help="histogram: the headline line; the others run one configuration of the suite alone "
                         "(its JSON object on one line; --steps sets its repetitions / heat iterations)")
     p.add_argument("--variant", type=int, default=-1,
@@ -248,30 +250,47 @@ def run_gpu(args):
     traffic = profile_traffic("weighted_histogram_i64_B%d" % dom)
 
     def run_e2e():
-        # e2e through the C-ABI host-pointer entry point: H2D of the step's input from
-        # pinned host memory and D2H of the histogram inside the timed region.
+        # e2e through the reference-ABI export hyd_export_weighted_histogram(hyd_array_t*,
+        # bins) (CodegenC.hs:411-425 shape).  The host's data is a hyd_array_t over pinned
+        # host memory, made device-resident once (hyd_cuda_array_attach).  Every step the
+        # host declares that it rewrote the data (hyd_cuda_array_host_modified), so the
+        # step's first export call uploads it (1 GiB H2D inside the timed region) and the
+        # second reads the resident copy; each call returns its bins in a new caller-owned
+        # host hyd_array_t (D2H), released with the reference's hyd_array_free protocol.
+        import ctypes
+        import numpy as np
         pinned = torch.empty(N_ELEMS, dtype=torch.int64, pin_memory=True)
         pinned.copy_(data)
-        out_host = {b: torch.zeros(b, dtype=torch.int64, pin_memory=True) for b in BINS}
+        arr = hc.make_array(pinned.numpy())
+        hc.check(L.hyd_cuda_array_attach(ctypes.byref(arr)))
         e2e_steps = max(3, min(args.steps, 20))
+        last = {}
 
-        def e2e_step():
+        def e2e_step(keep=False):
+            hc.check(L.hyd_cuda_array_host_modified(ctypes.byref(arr)))
             for b in BINS:
-                hc.check(L.hyd_cuda_weighted_histogram_host(pinned.data_ptr(), N_ELEMS, b,
-                                                            out_host[b].data_ptr(), 0))
+                p = hc.export_weighted_histogram(arr, b)
+                if keep:
+                    last[b] = np.ctypeslib.as_array(ctypes.cast(p.contents.data, ctypes.POINTER(ctypes.c_int64)),
+                                                    shape=(b,)).copy()
+                hc.array_free(p)
         for _ in range(2):
             e2e_step()
+        _, up0, _ = hc.resident_stats()
         if dist:
             dist.barrier()
         te = time.perf_counter()
-        for _ in range(e2e_steps):
-            e2e_step()
+        for k in range(e2e_steps):
+            e2e_step(keep=(k == e2e_steps - 1))
         e2e_s = time.perf_counter() - te
+        _, up1, _ = hc.resident_stats()
+        assert up1 - up0 == e2e_steps, "one upload per step expected"
         e2e_s = max_over_ranks(e2e_s, dist, dev)
         for b in BINS:
-            assert torch.equal(out_host[b], hists[b].cpu()), "e2e result differs"
+            assert np.array_equal(last[b], hists[b].cpu().numpy()), "e2e result differs"
+        hc.check(L.hyd_cuda_array_detach(ctypes.byref(arr)))
         e2e_value = whole_job_gbs(world, bytes_per_step, e2e_steps, e2e_s)
-        del pinned, out_host
+        del pinned, arr
         return e2e_value, e2e_steps
 
     e2e_value, e2e_steps = (None, 0) if args.no_e2e else run_e2e()
@@ -324,9 +343,11 @@ def run_gpu(args):
             },
             "e2e": None if e2e_value is None else {
                 "value": round(e2e_value, 2), "unit": "GB/s",
-                "h2d_bytes_per_step": 8 * N_ELEMS * len(BINS),
+                "h2d_bytes_per_step": 8 * N_ELEMS,
                 "d2h_bytes_per_step": 8 * sum(BINS),
-                "call": "hyd_cuda_weighted_histogram_host (pinned host input, 64 MiB chunks, 2 streams)",
+                "call": "hyd_export_weighted_histogram(hyd_array_t*, bins) for each B on a pinned host array "
+                        "kept device-resident; hyd_cuda_array_host_modified every step, so each step uploads "
+                        "the 1 GiB input once and both calls read it",
                 "steps": e2e_steps,
             },
             "gpu_launches": sum(plans[b][1] for b in BINS) * args.steps,
@@ -346,7 +367,49 @@ def run_gpu(args):
 # Correctness guards here use product code and size-independent properties; the
 # oracle only appears in the *_cpu_baseline helpers.
 # ----------------------------------------------------------------------------------
-FP64_DFMA_PER_S = 1.9 * 152 * 2.07e9  # measured on this GB300: 1.9 DFMA/clk/SM (1.2 TFLOP/s)
+def measure_fp64_peak(hc, torch, reps=20):
+    """The FP64 unit's issue rate on this device, measured: hyd_cuda_probe_fp64_rate
+    (eight independent fma chains per thread, four 256-thread blocks per SM),
+    CUDA-event timed on the launching stream, best of `reps`, with the SM clocks
+    sampled during the runs.  One fma counts as one FP64 operation, as every
+    FP64-bound roofline below counts them."""
+    import ctypes
+    dev = torch.device("cuda")
+    sink = torch.zeros(2, dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream()
+    L = hc.lib()
+    cnt = ctypes.c_int64(0)
+    iters = 1 << 14
+    hc.check(L.hyd_cuda_probe_fp64_rate(iters, sink.data_ptr(), ctypes.byref(cnt), s.cuda_stream))
+    torch.cuda.synchronize()
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    best = None
+    for _ in range(reps):
+        e0, e1 = _events(torch, s)
+        e0.record(s)
+        hc.check(L.hyd_cuda_probe_fp64_rate(iters, sink.data_ptr(), None, s.cuda_stream))
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None or ms < best else best
+    clocks = sampler.stop()
+    rate = cnt.value / (best / 1e3)
+    sms = hc.lib().hyd_cuda_device_sm_count()
+    out = {"fp64_ops_per_s": round(rate, 1), "sm_count": sms, "ms": round(best, 4), "fma_per_launch": cnt.value,
+           "how": "hyd_cuda_probe_fp64_rate: %d blocks x 256 threads x 8 independent fma chains x %d rounds, "
+                  "CUDA events, best of %d" % (4 * sms, iters, reps), "clocks": clocks}
+    if clocks and clocks.get("sm_mhz"):
+        out["per_sm_per_clk"] = round(rate / sms / (clocks["sm_mhz"] * 1e6), 3)
+    return out
+
+
+def _fp64_roofline(ops_per_unit, units_per_s, fp64):
+    achieved = ops_per_unit * units_per_s
+    peak = fp64["fp64_ops_per_s"] if fp64 else None
+    return {"bound": "fp64", "fp64_ops_per_unit": ops_per_unit, "achieved_fp64_ops_per_s": round(achieved, 1),
+            "peak_fp64_ops_per_s": peak, "peak_source": "measured in this run (hyd_cuda_probe_fp64_rate)",
+            "frac": round(achieved / peak, 3) if peak else None}
 
 
 def _events(torch, stream):
@@ -398,7 +461,7 @@ def _dot_cpu_baseline(O, hx, hy, gpu_value):
             "gpu_rel_err_vs_compensated": abs(gpu_value - ref) / max(1.0, abs(ref))}
 
 
-def suite_heat(hc, torch, peak, iters=1000, variant=-1):
+def suite_heat(hc, torch, peak, iters=1000, variant=-1, fp64=None):
     h = w = 8192
     dev = torch.device("cuda")
     b0 = torch.empty((h, w), dtype=torch.float64, device=dev)
@@ -444,23 +507,40 @@ def suite_heat(hc, torch, peak, iters=1000, variant=-1):
     # FP64-unit operations per point: 3 DADD + fma(-4,e,t) + DMUL + DADD, minus
     # the sum additions the chosen variant runs on the integer pipe
     emu = (0, 2, 3)[best // 7]
-    dp_ops = (6 - emu) * pts
-    return {"config": "heat_2d out = in + 0.1*lap(in), clamp, 8192^2 f64 U[0,1) seed 3, 1000 steps, CUDA graph",
-            "steps": iters, "autotuned": results["autotuned"], "fixed_32x32": results["fixed_32x32"],
-            "tune_times_us_per_variant": {str(hc.STENCIL_VARIANTS[i]): round(float(t), 1) for i, t in enumerate(times)},
-            "speedup_vs_fixed_32x32": round(results["fixed_32x32"]["total_ms"] / results["autotuned"]["total_ms"], 3),
-            "variants_bit_identical_after_1000_steps": same,
-            "effective_hbm_GB_s": round(hbm, 1), "frac_of_hbm_peak": round(hbm / peak, 3),
-            "roofline": {"bound": "fp64", "achieved_dfma_equiv_per_s": round(dp_ops / (ms_step / 1e3), 3),
-                         "peak_dp_ops_per_s": FP64_DFMA_PER_S,
-                         "frac": round(dp_ops / (ms_step / 1e3) / FP64_DFMA_PER_S, 3),
-                         "fp64_ops_per_point": 6 - emu, "integer_pipe_adds_per_point": emu,
-                         "points_per_s": round(pts / (ms_step / 1e3), 1),
-                         "note": "FP64 unit measured at 1.9 DFMA/clk/SM on this GB300; the variant runs %d of "
-                                 "the 6 per-point operations as exact integer-pipe additions" % emu}}
+    roof = _fp64_roofline(6 - emu, pts / (ms_step / 1e3), fp64)
+    roof.update({"integer_pipe_adds_per_point": emu, "points_per_s": round(pts / (ms_step / 1e3), 1),
+                 "note": "the variant runs %d of the 6 per-point operations as exact integer-pipe additions" % emu})
+    res = {"config": "heat_2d out = in + 0.1*lap(in), clamp, 8192^2 f64 U[0,1) seed 3, 1000 steps, CUDA graph",
+           "steps": iters, "autotuned": results["autotuned"], "fixed_32x32": results["fixed_32x32"],
+           "tune_times_us_per_variant": {str(hc.STENCIL_VARIANTS[i]): round(float(t), 1) for i, t in enumerate(times)},
+           "speedup_vs_fixed_32x32": round(results["fixed_32x32"]["total_ms"] / results["autotuned"]["total_ms"], 3),
+           "variants_bit_identical_after_1000_steps": same,
+           "effective_hbm_GB_s": round(hbm, 1), "frac_of_hbm_peak": round(hbm / peak, 3),
+           "roofline": roof}
+    try:
+        from oracle import oracle as O
+        res["cpu_baseline"] = _heat_cpu_baseline(O, init.cpu().numpy(), results["autotuned"]["ms_per_step"])
+    except Exception as e:
+        res["cpu_baseline"] = {"error": str(e)}
+    return res
 
 
-def suite_map_chain(hc, torch, peak, steps=20):
+def _heat_cpu_baseline(O, grid, gpu_ms_per_step, steps=10):
+    """The oracle's split-region clamp stencil + ping-pong iterate (the C
+    backend's loops, OpenMP over rows) on the host cores: `steps` steps of the
+    full 8192^2 grid from the workload's initial state."""
+    O.iterate_stencil2d(O.HEAT, grid, 1)  # warm-up
+    t = time.perf_counter()
+    O.iterate_stencil2d(O.HEAT, grid, steps)
+    dt = time.perf_counter() - t
+    pts = grid.size
+    return {"value": round(16 * pts * steps / dt / 1e9, 3), "unit": "GB/s", "cores": O.lib().orc_max_threads(),
+            "kind": "port", "ms_per_step": round(1e3 * dt / steps, 3),
+            "gpu_speedup": round(1e3 * dt / steps / gpu_ms_per_step, 1),
+            "sample": "%d steps of the full 8192^2 grid (effective GB/s = 16 B per point per step)" % steps}
+
+
+def suite_map_chain(hc, torch, peak, steps=20, fp64=None):
     """bench/map_chain/map_chain.hyd: reduce (+) over generate (i/n) -> x*x ->
     x-0.5 -> x*2+1, n = 2^27, one fused run-time-compiled kernel (no memory
     traffic: the chain is generated)."""
@@ -482,11 +562,58 @@ def suite_map_chain(hc, torch, peak, steps=20):
     return {"config": "map_chain reduce(+) (map (x*2+1) (map (x-0.5) (map (x*x) (generate [n] (i/n))))), n=2^27 f64",
             "ms": round(ms, 4), "Gelem_s": round(n / (ms / 1e3) / 1e9, 2), "sum": ssum.item(),
             "rel_err_vs_exact": abs(ssum.item() - exact) / abs(exact),
-            "note": "compute only (generated input); about seven FP64 operations per element on GB300's FP64 unit "
-                    "(1.9/clk/SM) bound it; the division by the power of two n runs as the exact multiply"}
+            "roofline": _fp64_roofline(7, n / (ms / 1e3), fp64),
+            "note": "compute only (generated input); seven FP64 operations per element bound it (the conversion "
+                    "of i, the division by the power of two n as the exact multiply, three multiplies and two "
+                    "additions of the chain, the reduction's addition)"}
 
 
-def suite_jacobi1d(hc, torch, peak, iters=100):
+def suite_map_zipwith(hc, torch, peak, steps=20):
+    """A memory-bound fused chain: zipwith (+.) (zipwith ( *. ) a b) c over three
+    resident float64 inputs of 2^27 elements (1 GiB each) into a fourth, one
+    run-time-compiled kernel; 32 B of HBM traffic per element."""
+    n = 1 << 27
+    dev = torch.device("cuda")
+    xs = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(3)]
+    for k, t in enumerate(xs):
+        hc.fill_uniform_f64(t, 21 + k, -1.0, 1.0)
+    out = torch.empty(n, dtype=torch.float64, device=dev)
+    body = "v = x0 * x1 + x2;"
+    for _ in range(3):
+        hc.map_f64(body, xs, out=out)  # the first call compiles
+    s = torch.cuda.current_stream()
+    e0, e1 = _events(torch, s)
+    e0.record(s)
+    for _ in range(steps):
+        hc.map_f64(body, xs, out=out)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    same = bool(torch.equal(out, torch.add(torch.mul(xs[0], xs[1]), xs[2])))  # two roundings, as the C loop
+    gbs = 32 * n / (ms / 1e3) / 1e9
+    res = {"config": "zipwith (+.) (zipwith (*.) a b) c, n=2^27 f64 each, U[-1,1) seeds 21..23, resident; "
+                     "inputs larger than L2",
+           "ms": round(ms, 4), "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3),
+           "algorithmic_bytes": 32 * n, "launches_per_step": 1, "elements_match_two_rounding_reference": same}
+    try:
+        from oracle import oracle as O
+        ha = [t.cpu().numpy() for t in xs]
+        del xs, out
+        O.zipwith_muladd(*ha)  # warm-up
+        t = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            O.zipwith_muladd(*ha)
+        dt = (time.perf_counter() - t) / reps
+        res["cpu_baseline"] = {"value": round(32 * n / dt / 1e9, 2), "unit": "GB/s",
+                               "cores": O.lib().orc_max_threads(), "kind": "port",
+                               "sample": "full n, %d reps of the fused OpenMP loop" % reps}
+    except Exception as e:
+        res["cpu_baseline"] = {"error": str(e)}
+    return res
+
+
+def suite_jacobi1d(hc, torch, peak, iters=100, fp64=None):
     """jacobi_1d (examples/jacobi_1d.hyd) over n = 2^25 float64, a captured graph."""
     n = 1 << 25
     dev = torch.device("cuda")
@@ -507,11 +634,120 @@ def suite_jacobi1d(hc, torch, peak, iters=100):
     return {"config": "jacobi_1d (a[i-1] + a[i] + a[i+1]) / 3.0 clamp, n=2^25 f64 U[0,1) seed 7, %d steps, CUDA graph"
                       % iters, "ms_per_step": round(ms, 4), "GB_s": round(gbs, 1),
             "frac_of_hbm_peak": round(gbs / peak, 3),
-            "note": "FP64-unit-bound on GB300 (1.9 DFMA/clk/SM): two sums on the integer pipe, the division by 3 "
-                    "as one multiply and two FMAs (bit-identical to IEEE division)"}
+            "roofline": _fp64_roofline(3, n / (ms / 1e3), fp64),
+            "note": "three FP64 operations per point: the division by 3 as one multiply and two FMAs "
+                    "(bit-identical to IEEE division); both sums run on the integer pipe"}
 
 
-def suite_gray_scott(hc, torch, peak, steps=5000):
+def suite_scan(hc, torch, peak, steps=20):
+    """scan (+) over 2^27 elements, float64 and int64, exclusive, resident:
+    one single-pass decoupled look-back kernel each, 16 B of HBM traffic per
+    element (one read, one write)."""
+    import numpy as np
+    n = 1 << 27
+    dev = torch.device("cuda")
+    s = torch.cuda.current_stream()
+    out = {}
+    for name, dtype in (("f64", torch.float64), ("i64", torch.int64)):
+        x = torch.empty(n, dtype=dtype, device=dev)
+        if dtype == torch.float64:
+            hc.fill_uniform_f64(x, 41, -1.0, 1.0)
+            init = 0.5
+        else:
+            hc.fill_uniform_i64(x, 41, 1 << 40)
+            init = 7
+        y = torch.empty_like(x)
+        for _ in range(3):
+            hc.scan(x, y, init)
+        first = y.clone()
+        e0, e1 = _events(torch, s)
+        e0.record(s)
+        for _ in range(steps):
+            hc.scan(x, y, init)
+        e1.record(s)
+        torch.cuda.synchronize()
+        hc.check(hc.device_check())
+        ms = e0.elapsed_time(e1) / steps
+        gbs = 16 * n / (ms / 1e3) / 1e9
+        res = {"ms": round(ms, 4), "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3),
+               "run_to_run_identical": bool(torch.equal(first, y))}
+        if dtype == torch.int64:
+            tot = int(x.cpu().numpy().astype(np.uint64).sum(dtype=np.uint64))
+            last = int(y[-1].item()) + int(x[-1].item())
+            res["total_matches"] = (last - init - tot) % (1 << 64) == 0
+        else:
+            from oracle import oracle as O
+            h = x.cpu().numpy()
+            exact = O.sum_compensated(h) + init
+            res["total_rel_err"] = abs(float(y[-1].item()) + float(x[-1].item()) - exact) / \
+                max(1.0, float(np.abs(h).sum()))
+            t = time.perf_counter()
+            O.scan_f64(h, init)
+            dt = time.perf_counter() - t
+            res["cpu_baseline"] = {"value": round(16 * n / dt / 1e9, 3), "unit": "GB/s", "cores": 1,
+                                   "kind": "port", "sample": "full n, the serial fold (the C backend never "
+                                                             "parallelises a fold)"}
+        out[name] = res
+        del x, y, first
+    out["config"] = "scan (+) exclusive, n=2^27, f64 U[-1,1) / i64 U[0,2^40) seed 41, resident; inputs larger than L2"
+    return out
+
+
+def suite_segmented_reduce(hc, torch, peak, steps=20):
+    """segmented_reduce (+) over 2^27 float64 values with skewed segment lengths
+    (floor(2^U(0,16)), seed 43): many short segments and a long tail of long
+    ones; tiles of values with a deterministic carry look-back."""
+    import numpy as np
+    n = 1 << 27
+    rng = np.random.default_rng(43)
+    lens = np.floor(2.0 ** rng.uniform(0, 16, size=n // 1000)).astype(np.int64)
+    cum = np.cumsum(lens)
+    k = int(np.searchsorted(cum, n))
+    lens = lens[:k + 1]
+    lens[-1] -= int(cum[k] - n) if k < len(cum) else 0
+    offsets = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    offsets[-1] = n
+    nseg = len(offsets) - 1
+    dev = torch.device("cuda")
+    vals = torch.empty(n, dtype=torch.float64, device=dev)
+    hc.fill_uniform_f64(vals, 43, -1.0, 1.0)
+    d_off = torch.from_numpy(offsets).to(dev)
+    outv = torch.empty(nseg, dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        hc.segmented_reduce(d_off, vals, outv, init=0.0)
+    first = outv.clone()
+    e0, e1 = _events(torch, s)
+    e0.record(s)
+    for _ in range(steps):
+        hc.segmented_reduce(d_off, vals, outv, init=0.0)
+    e1.record(s)
+    torch.cuda.synchronize()
+    hc.check(hc.device_check())
+    ms = e0.elapsed_time(e1) / steps
+    alg = 8 * n + 8 * (nseg + 1) + 8 * nseg
+    gbs = alg / (ms / 1e3) / 1e9
+    res = {"config": "segmented_reduce (+) 0.0, 2^27 f64 values U[-1,1) seed 43, %d segments of floor(2^U(0,16)) "
+                     "values (seed 43), longest %d" % (nseg, int(lens.max())),
+           "segments": nseg, "ms": round(ms, 4), "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3),
+           "algorithmic_bytes": alg, "run_to_run_identical": bool(torch.equal(first, outv)),
+           "launches_per_step": 2, "note": "tile kernel + a per-segment pass that exits at once for valid offsets"}
+    try:
+        from oracle import oracle as O
+        hv = vals.cpu().numpy()
+        t = time.perf_counter()
+        ref = O.segmented_reduce_f64(offsets, hv, 0.0)
+        dt = time.perf_counter() - t
+        absum = O.segmented_reduce_f64(offsets, np.abs(hv), 0.0)
+        res["max_err_over_abs_sum"] = float(np.max(np.abs(outv.cpu().numpy() - ref) / np.maximum(absum, 1.0)))
+        res["cpu_baseline"] = {"value": round(alg / dt / 1e9, 3), "unit": "GB/s", "cores": O.lib().orc_max_threads(),
+                               "kind": "port", "sample": "full workload, schedule(dynamic) per segment"}
+    except Exception as e:
+        res["cpu_baseline"] = {"error": str(e)}
+    return res
+
+
+def suite_gray_scott(hc, torch, peak, steps=5000, fp64=None):
     """Gray-Scott (demo/gray_scott/gray_scott.hyd): the demo's 256^2 x 5000 steps
     (launch-bound: a captured graph) and a 4096^2 grid (throughput)."""
     import numpy as np
@@ -533,7 +769,8 @@ def suite_gray_scott(hc, torch, peak, steps=5000):
         ms = e0.elapsed_time(e1)
         gbs = 32 * h * w * k / (ms / 1e3) / 1e9
         out["%dx%d" % (h, w)] = {"steps": k, "total_ms": round(ms, 3), "us_per_step": round(1e3 * ms / k, 2),
-                                 "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3)}
+                                 "GB_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3),
+                                 "roofline": _fp64_roofline(17, h * w * k / (ms / 1e3), fp64)}
         del bufs
     out["config"] = "gray_scott U,V periodic, du 0.21 dv 0.105 feed 0.0545 kill 0.062 dt 1, CUDA graph"
     return out
@@ -702,9 +939,20 @@ def suite_serve(hc, torch, peak, nreq=100_000, lam=20_000.0):
 
 def run_suite(hc, torch, args, peak):
     out = {}
-    for name, fn in (("dot", suite_dot), ("map_chain", suite_map_chain), ("heat_2d", suite_heat),
-                     ("jacobi_1d", suite_jacobi1d),
-                     ("gray_scott", suite_gray_scott), ("batched_coo_csr_spmv", suite_batched),
+    try:
+        fp64 = measure_fp64_peak(hc, torch)
+    except Exception as e:
+        fp64 = None
+        out["fp64_peak"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    else:
+        out["fp64_peak"] = fp64
+    for name, fn in (("dot", suite_dot), ("map_zipwith", suite_map_zipwith),
+                     ("map_chain", lambda a, b, c: suite_map_chain(a, b, c, fp64=fp64)),
+                     ("heat_2d", lambda a, b, c: suite_heat(a, b, c, fp64=fp64)),
+                     ("jacobi_1d", lambda a, b, c: suite_jacobi1d(a, b, c, fp64=fp64)),
+                     ("gray_scott", lambda a, b, c: suite_gray_scott(a, b, c, fp64=fp64)),
+                     ("scan", suite_scan), ("segmented_reduce", suite_segmented_reduce),
+                     ("batched_coo_csr_spmv", suite_batched),
                      ("serving", lambda a, b, c: suite_serve(a, b, c, nreq=args.serve_requests))):
         t = time.perf_counter()
         try:
@@ -789,16 +1037,24 @@ def run_one(args):
     hc = g.package()
     hc.check(hc.lib().hyd_cuda_init())
     peak = measured_peak()[0]
+    fp64 = measure_fp64_peak(hc, torch) if args.workload in ("heat", "map_chain", "jacobi1d", "gray_scott") \
+        else None
     if args.workload == "dot":
         res = suite_dot(hc, torch, peak, steps=args.steps)
     elif args.workload == "heat":
-        res = suite_heat(hc, torch, peak, iters=args.steps, variant=args.variant)
+        res = suite_heat(hc, torch, peak, iters=args.steps, variant=args.variant, fp64=fp64)
     elif args.workload == "map_chain":
-        res = suite_map_chain(hc, torch, peak, steps=args.steps)
+        res = suite_map_chain(hc, torch, peak, steps=args.steps, fp64=fp64)
+    elif args.workload == "map_zipwith":
+        res = suite_map_zipwith(hc, torch, peak, steps=args.steps)
     elif args.workload == "jacobi1d":
-        res = suite_jacobi1d(hc, torch, peak, iters=args.steps)
+        res = suite_jacobi1d(hc, torch, peak, iters=args.steps, fp64=fp64)
     elif args.workload == "gray_scott":
-        res = suite_gray_scott(hc, torch, peak, steps=args.steps)
+        res = suite_gray_scott(hc, torch, peak, steps=args.steps, fp64=fp64)
+    elif args.workload == "scan":
+        res = suite_scan(hc, torch, peak, steps=args.steps)
+    elif args.workload == "segreduce":
+        res = suite_segmented_reduce(hc, torch, peak, steps=args.steps)
     elif args.workload == "batched":
         res = suite_batched(hc, torch, peak, steps=args.steps, instances=args.instances)
     else:

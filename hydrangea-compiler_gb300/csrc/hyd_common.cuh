@@ -189,9 +189,11 @@ __device__ __forceinline__ bool mbar_test_wait(unsigned addr, unsigned parity) {
     return ok != 0;
 }
 // Bounded wait (non-blocking polls with a short sleep between them, about a
-// quarter of a second in total); false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity) {
-    for (unsigned it = 0; it < kTmaWaitLimit; ++it) {
+// quarter of a second in total at the default limit); false when the limit ran
+// out.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity,
+                                                  unsigned limit = kTmaWaitLimit) {
+    for (unsigned it = 0; it < limit; ++it) {
         if (mbar_test_wait(addr, parity)) return true;
         __nanosleep(64);
     }
@@ -204,6 +206,30 @@ __device__ __forceinline__ void bulk_load_1d(unsigned dst, const void* src, unsi
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
         "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(mbar)
         : "memory");
+}
+
+// ---- decoupled look-back: bounded wait on a window of tile status flags -------
+constexpr unsigned kSpinLimit = 1u << 22;  // polls before a look-back gives up
+
+__device__ __forceinline__ unsigned ld_volatile_u32(const unsigned* p) { return *(volatile const unsigned*)p; }
+
+// Warp-wide: lane l watches the status flag of tile q = p - l (q < 0: before
+// the first tile, reported as 2 = "inclusive prefix known").  Polls until every
+// lane's flag is non-zero and returns this lane's flag, or returns 0 on every
+// lane when `limit` polls went by without that (the caller raises
+// ERRBIT_TIMEOUT and abandons the look-back).  Flags are published with a
+// __threadfence() before the volatile store, so the caller fences once after a
+// successful return before reading the published values.
+__device__ __forceinline__ unsigned lookback_wait_window(const unsigned* flags, int64_t p, int lane,
+                                                         unsigned limit = kSpinLimit) {
+    const int64_t q = p - lane;
+    unsigned f = q >= 0 ? ld_volatile_u32(&flags[q]) : 2u;
+    unsigned spins = 0;
+    while (__any_sync(0xffffffffu, f == 0u)) {
+        if (++spins > limit) return 0u;
+        if (f == 0u) f = ld_volatile_u32(&flags[q]);
+    }
+    return f;
 }
 
 }  // namespace hyd

@@ -15,10 +15,27 @@
 // wrap and commute, so the result is bit-identical to the serial C fold.
 // One read and one write per element: 16 B/element of HBM traffic.
 //
-// float64: reduce-then-scan in three launches with a fixed combine order, so
-// results are run-to-run reproducible.  A parallel prefix cannot reproduce the
-// serial fold's roundings; the tolerance is |gpu - c| <= 1e-12 * prefix sum of
-// |x| (stated in the tests).
+// float64: single-pass decoupled look-back with a deterministic combine.  A
+// tile publishes its aggregate, then looks back to the nearest predecessor
+// that has published an inclusive prefix and folds the aggregates in between
+// onto it left to right (lookback_fold).  Every inclusive prefix is made that
+// way, so each equals the left fold of all earlier tile aggregates onto init,
+// whatever the timing: results are run-to-run identical.  Within a tile the
+// order is fixed too (per-thread serial sums, a fixed shuffle tree).  A
+// parallel prefix cannot reproduce the serial fold's roundings; the tolerance
+// is |gpu - c| <= 1e-12 * prefix sum of |x| (stated in the tests).
+//
+// segmented_reduce: tiles of 4096 values (not one warp per segment), so a long
+// segment is spread over many CTAs and many short ones share one.  A warp
+// finds the tile's segments with a 32-ary search of the offsets; a segmented
+// scan of the tile (head flags at segment starts, fixed shuffle tree) gives
+// every segment that ends in the tile its sum; the segment still open at the
+// tile's start gets its carry from the predecessors through the same
+// deterministic look-back (a tile that holds a segment start is an inclusive
+// prefix at once, so the look-back stops there).  One read of offsets and
+// values, one write of the sums.  Offsets that are not a non-decreasing
+// partition of [0, n_vals] are detected by the tiles and handed to a per-
+// segment kernel that gives the reference semantics (init, error reported).
 //
 // Reverse scans read and write index n-1-k for logical position k, exactly the
 // ix the reference's lowering computes.
@@ -29,7 +46,6 @@ namespace hyd {
 constexpr int kScanT = 512;
 constexpr int kScanIPT = 8;
 constexpr int kScanTile = kScanT * kScanIPT;  // 4096 (32 KiB of static shared memory for int64)
-constexpr unsigned kSpinLimit = 1u << 22;
 
 // --- block-wide exclusive scan of one value per thread (int64, wrapping) ------
 template <class T>
@@ -67,12 +83,14 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* sh /*[32]*/, T& total)
 template <class T>
 __device__ __forceinline__ void tile_load(const T* in, int64_t n, int64_t base, bool reverse, T* sh,
                                           T (&items)[kScanIPT]) {
-    for (int i = threadIdx.x; i < kScanTile; i += kScanT) {
-        const int64_t k = base + i;
-        T v = T(0);
-        if (k < n) v = in[reverse ? (n - 1 - k) : k];
-        sh[i] = v;
+    T v[kScanIPT];
+#pragma unroll
+    for (int j = 0; j < kScanIPT; ++j) {  // all loads in flight before the first store
+        const int64_t k = base + threadIdx.x + j * kScanT;
+        v[j] = k < n ? in[reverse ? (n - 1 - k) : k] : T(0);
     }
+#pragma unroll
+    for (int j = 0; j < kScanIPT; ++j) sh[threadIdx.x + j * kScanT] = v[j];
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < kScanIPT; ++j) items[j] = sh[threadIdx.x * kScanIPT + j];
@@ -100,7 +118,6 @@ struct ScanStatus {
     unsigned* tile_counter;
 };
 
-__device__ __forceinline__ unsigned ld_volatile_u32(const unsigned* p) { return *(volatile const unsigned*)p; }
 __device__ __forceinline__ long long ld_volatile_i64(const long long* p) { return *(volatile const long long*)p; }
 
 __global__ void __launch_bounds__(kScanT) scan_i64_lookback_kernel(const long long* __restrict__ in,
@@ -144,16 +161,11 @@ __global__ void __launch_bounds__(kScanT) scan_i64_lookback_kernel(const long lo
             long long running = 0;
             int64_t p = (int64_t)tile - 1;  // window covers p, p-1, ..., p-31
             bool done = false;
-            unsigned spins = 0;
             while (!done) {
                 const int64_t q = p - lane;
-                unsigned f = q >= 0 ? ld_volatile_u32(&st.flag[q]) : 2u;
                 // wait until every tile of the window has published something
-                while (__any_sync(0xffffffffu, f == 0u)) {
-                    if (++spins > kSpinLimit) break;
-                    if (f == 0u) f = ld_volatile_u32(&st.flag[q]);
-                }
-                if (spins > kSpinLimit) {
+                const unsigned f = lookback_wait_window(st.flag, p, lane);
+                if (f == 0u) {
                     if (lane == 0) raise_error(err, ERRBIT_TIMEOUT);
                     break;
                 }
@@ -195,89 +207,326 @@ __global__ void __launch_bounds__(kScanT) scan_i64_lookback_kernel(const long lo
     tile_store(out, n, base, reverse, sh_tile, items);
 }
 
-// ---- float64 reduce-then-scan ------------------------------------------------------
-__device__ __forceinline__ double block_sum_f64(double v, double* sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[warp] = v;
+// ---- deterministic decoupled look-back (left fold) -----------------------------------
+// Status per tile: flag (0 none, 1 aggregate, 2 inclusive) and the two values.
+template <class T>
+struct FoldStatus {
+    unsigned* flag;
+    T* aggregate;
+    T* inclusive;
+    unsigned* tile_counter;
+    unsigned* bad;  // segmented reduce: the offsets are not a valid partition
+};
+constexpr int kFoldBuf = 1024;                // aggregates one look-back may collect before it restarts
+constexpr unsigned kFoldRestarts = 1u << 12;  // restarts before a look-back gives up
+
+template <class T>
+__device__ __forceinline__ T ld_volatile(const T* p) {
+    return *(volatile const T*)p;
+}
+
+// Warp-wide (all 32 lanes of one warp).  The exclusive prefix of `tile`, as
+// the left fold inclusive[s] + aggregate[s+1] + ... + aggregate[tile-1] where s
+// is the nearest predecessor that has published an inclusive value (`before`
+// stands for the inclusive value of tile -1).  Every inclusive value is made
+// the same way, so the result is the left fold of all earlier aggregates,
+// whatever the timing.  Aggregates are collected in sbuf (kFoldBuf); when the
+// nearest inclusive predecessor is further back than that, the look-back
+// starts again from tile - 1 (nearer prefixes will have appeared by then).
+// Returns false on every lane when a wait ran out.
+template <class T>
+__device__ bool lookback_fold(const FoldStatus<T>& st, int64_t tile, T before, T* sbuf, T& prefix) {
+    const int lane = threadIdx.x & 31;
+    unsigned restarts = 0;
+    int64_t p = tile - 1;
+    int cnt = 0;
+    T base = before;
+    for (;;) {
+        const unsigned f = lookback_wait_window(st.flag, p, lane);
+        if (f == 0u) return false;
+        __threadfence();
+        const int64_t q = p - lane;
+        const unsigned incl = __ballot_sync(0xffffffffu, f == 2u);
+        const int stop = incl ? __ffs(incl) - 1 : 32;
+        if (lane < stop) sbuf[cnt + lane] = ld_volatile(&st.aggregate[q]);
+        if (stop < 32) {
+            T b = before;
+            if (lane == stop && q >= 0) b = ld_volatile(&st.inclusive[q]);
+            base = __shfl_sync(0xffffffffu, b, stop);
+            cnt += stop;
+            break;
+        }
+        cnt += 32;
+        p -= 32;
+        if (cnt + 32 > kFoldBuf) {
+            if (++restarts > kFoldRestarts) return false;
+            cnt = 0;
+            p = tile - 1;
+            __nanosleep(256);
+        }
+    }
+    __syncwarp();
+    T acc = base;
+    if (lane == 0)
+        for (int i = cnt - 1; i >= 0; --i) acc = acc + sbuf[i];
+    prefix = __shfl_sync(0xffffffffu, acc, 0);
+    return true;
+}
+
+// float64 (and any T) scan with the left-fold look-back.
+template <class T>
+__global__ void __launch_bounds__(kScanT) scan_fold_kernel(const T* __restrict__ in, T* __restrict__ out, int64_t n,
+                                                            T init, bool reverse, bool inclusive, FoldStatus<T> st,
+                                                            unsigned* err) {
+    __shared__ T sh_tile[kScanTile];
+    __shared__ T sh_scan[33];
+    __shared__ T sh_fold[kFoldBuf];
+    __shared__ unsigned sh_tile_id;
+    __shared__ T sh_prefix;
+    if (threadIdx.x == 0) sh_tile_id = atomicAdd(st.tile_counter, 1u);
     __syncthreads();
-    double r = 0.0;
-    if (warp == 0) {
-        r = lane < nw ? sh[lane] : 0.0;
+    const unsigned tile = sh_tile_id;
+    const int64_t base = (int64_t)tile * kScanTile;
+    T items[kScanIPT];
+    tile_load(in, n, base, reverse, sh_tile, items);
+    T tsum = items[0];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    for (int j = 1; j < kScanIPT; ++j) tsum = tsum + items[j];
+    T agg;
+    const T texcl = block_exclusive_scan(tsum, sh_scan, agg);
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        if (tile == 0) {
+            if (lane == 0) {
+                st.inclusive[0] = init + agg;
+                __threadfence();
+                *(volatile unsigned*)&st.flag[0] = 2u;
+                sh_prefix = init;
+            }
+        } else {
+            if (lane == 0) {
+                st.aggregate[tile] = agg;
+                __threadfence();
+                *(volatile unsigned*)&st.flag[tile] = 1u;
+            }
+            T prefix = T(0);
+            if (!lookback_fold(st, tile, init, sh_fold, prefix) && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
+            if (lane == 0) {
+                st.inclusive[tile] = prefix + agg;
+                __threadfence();
+                *(volatile unsigned*)&st.flag[tile] = 2u;
+                sh_prefix = prefix;
+            }
+        }
     }
     __syncthreads();
-    return r;  // valid in thread 0
-}
-
-__global__ void __launch_bounds__(kScanT) scan_f64_tile_sums_kernel(const double* __restrict__ in, int64_t n,
-                                                                     bool reverse, double* tile_sums) {
-    __shared__ double sh_tile[kScanTile];
-    __shared__ double sh[32];
-    const int64_t base = (int64_t)blockIdx.x * kScanTile;
-    double items[kScanIPT];
-    tile_load(in, n, base, reverse, sh_tile, items);
-    double t = 0.0;
-#pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) t += items[j];
-    const double s = block_sum_f64(t, sh);
-    if (threadIdx.x == 0) tile_sums[blockIdx.x] = s;
-}
-
-// One block: exclusive scan of the tile sums in a fixed order, seeded with init.
-__global__ void __launch_bounds__(1024) scan_f64_tile_prefix_kernel(double* tile_sums, int64_t ntiles,
-                                                                     double init) {
-    __shared__ double sh[33];
-    const int64_t per = (ntiles + blockDim.x - 1) / blockDim.x;
-    const int64_t b = (int64_t)threadIdx.x * per;
-    double s = 0.0;
-    for (int64_t i = b; i < b + per && i < ntiles; ++i) s += tile_sums[i];
-    double total;
-    double ex = block_exclusive_scan(s, sh, total);
-    double acc = init + ex;
-    for (int64_t i = b; i < b + per && i < ntiles; ++i) {
-        const double v = tile_sums[i];
-        tile_sums[i] = acc;
-        acc += v;
-    }
-}
-
-__global__ void __launch_bounds__(kScanT) scan_f64_downsweep_kernel(const double* __restrict__ in,
-                                                                     double* __restrict__ out, int64_t n,
-                                                                     bool reverse, bool inclusive,
-                                                                     const double* tile_prefix) {
-    __shared__ double sh_tile[kScanTile];
-    __shared__ double sh[33];
-    const int64_t base = (int64_t)blockIdx.x * kScanTile;
-    double items[kScanIPT];
-    tile_load(in, n, base, reverse, sh_tile, items);
-    double t = 0.0;
-#pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) t += items[j];
-    double total;
-    const double ex = block_exclusive_scan(t, sh, total);
-    double acc = tile_prefix[blockIdx.x] + ex;
+    T acc = sh_prefix + texcl;
 #pragma unroll
     for (int j = 0; j < kScanIPT; ++j) {
-        const double x = items[j];
+        const T x = items[j];
         if (inclusive) {
-            acc += x;
+            acc = acc + x;
             items[j] = acc;
         } else {
             items[j] = acc;
-            acc += x;
+            acc = acc + x;
         }
     }
     tile_store(out, n, base, reverse, sh_tile, items);
 }
 
-// ---- segmented reduce: one warp per segment -----------------------------------------
+// ---- segmented reduce over tiles of values ----------------------------------------------
+// First index i in [lo, hi) with a[i] >= key (a non-decreasing), else hi.
+// Warp-wide: 32 probes per round narrow the range 33-fold, about six dependent
+// loads for 2^27 offsets.  Monotone in `key` even for unsorted `a` (a larger
+// key never ends left of a smaller one), so tiles' ranges never overlap.
+__device__ __forceinline__ int64_t warp_lower_bound(const int64_t* a, int64_t lo, int64_t hi, int64_t key) {
+    const int lane = threadIdx.x & 31;
+    while (hi - lo > 32) {
+        const int64_t span = hi - lo;
+        const int64_t p = lo + span * (lane + 1) / 33;  // strictly inside (lo, hi), increasing in lane
+        const unsigned m = __ballot_sync(0xffffffffu, a[p] < key);
+        const int k = __popc(m);
+        const int64_t nlo = k ? lo + span * k / 33 + 1 : lo;
+        const int64_t nhi = k < 32 ? lo + span * (k + 1) / 33 : hi;
+        lo = nlo;
+        hi = nhi;
+    }
+    const bool below = lo + lane < hi && a[lo + lane] < key;
+    return lo + __popc(__ballot_sync(0xffffffffu, below));
+}
+
+// (head, value) pairs of a segmented scan: combine(a, b) = (a.h | b.h, b.h ? b.v : a.v + b.v).
+template <class T>
+__device__ __forceinline__ void seg_combine(bool& h, T& v, bool h_before, T v_before) {
+    if (!h) v = v_before + v;
+    h = h || h_before;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kScanT) segreduce_tile_kernel(const int64_t* __restrict__ offsets, int64_t nseg,
+                                                                 const T* __restrict__ vals, int64_t n_vals, T init,
+                                                                 T* __restrict__ out, FoldStatus<T> st,
+                                                                 int64_t ntiles, unsigned* err) {
+    __shared__ T sh_run[kScanTile];  // the tile's values, then the running segment sums
+    __shared__ unsigned sh_head[kScanTile / 32];
+    __shared__ T sh_fold[kFoldBuf];
+    __shared__ T sh_wv[32];
+    __shared__ unsigned sh_wh;
+    __shared__ int64_t sh_sb, sh_se;
+    __shared__ unsigned sh_tile_id;
+    __shared__ T sh_carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) sh_tile_id = atomicAdd(st.tile_counter, 1u);
+    if (threadIdx.x < kScanTile / 32) sh_head[threadIdx.x] = 0u;
+    __syncthreads();
+    const int64_t tile = sh_tile_id;
+    const int64_t v0 = tile * kScanTile;
+    const int cnt = (int)(n_vals - v0 < kScanTile ? n_vals - v0 : kScanTile);  // >= 0
+    const bool last = tile == ntiles - 1;
+    // the segments starting in this tile: [sb, se)
+    if (warp == 0) {
+        const int64_t sb = tile == 0 ? 0 : warp_lower_bound(offsets, 0, nseg, v0);
+        if (lane == 0) sh_sb = sb;
+    } else if (warp == 1) {
+        const int64_t se = last ? nseg : warp_lower_bound(offsets, 0, nseg, v0 + kScanTile);
+        if (lane == 0) sh_se = se;
+    }
+    {
+        T v[kScanIPT];
+#pragma unroll
+        for (int j = 0; j < kScanIPT; ++j) {
+            const int i = threadIdx.x + j * kScanT;
+            v[j] = i < cnt ? vals[v0 + i] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < kScanIPT; ++j) sh_run[threadIdx.x + j * kScanT] = v[j];
+    }
+    __syncthreads();
+    const int64_t sb = sh_sb, se = sh_se;
+    // head flags; every (offsets[s], offsets[s + 1]) pair of this tile's range is checked
+    bool bad = se < sb;
+    for (int64_t s = sb + threadIdx.x; s < se; s += kScanT) {
+        const int64_t o = offsets[s], e = offsets[s + 1];
+        const bool ok = o >= v0 && (last ? o <= n_vals : o < v0 + kScanTile) && e >= o && e <= n_vals;
+        bad |= !ok;
+        if (ok && o - v0 < cnt) atomicOr(&sh_head[(o - v0) >> 5], 1u << ((o - v0) & 31));
+    }
+    // the segment open at the tile's start (begun in an earlier tile) ends at offsets[sb]
+    const int64_t end_open = sb <= nseg ? offsets[sb] : 0;
+    const bool open = tile > 0 && sb > 0 && end_open > v0;
+    bad |= sb > nseg || (open && (end_open < v0 || end_open > n_vals));
+    if (__syncthreads_or(bad)) {
+        if (threadIdx.x == 0) {
+            atomicOr(st.bad, 1u);
+            st.inclusive[tile] = T(0);  // successors must not wait; the per-segment pass redoes every sum
+            __threadfence();
+            *(volatile unsigned*)&st.flag[tile] = 2u;
+        }
+        return;
+    }
+    // segmented scan of the tile: thread t owns positions 8t .. 8t+7
+    const int p0 = threadIdx.x * kScanIPT;
+    const unsigned hb = (sh_head[p0 >> 5] >> (p0 & 31)) & 0xffu;
+    T x[kScanIPT];
+#pragma unroll
+    for (int j = 0; j < kScanIPT; ++j) x[j] = sh_run[p0 + j];
+    bool h = hb != 0u;
+    T v = T(0);
+#pragma unroll
+    for (int j = 0; j < kScanIPT; ++j) v = (hb >> j) & 1u ? x[j] : v + x[j];
+    // inclusive warp scan of (h, v), then exclusive across warps
+    bool hi_ = h;
+    T vi = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const bool hu = __shfl_up_sync(0xffffffffu, hi_, d);
+        const T vu = __shfl_up_sync(0xffffffffu, vi, d);
+        if (lane >= d) seg_combine(hi_, vi, hu, vu);
+    }
+    const unsigned whead = __ballot_sync(0xffffffffu, h);
+    if (lane == 31) sh_wv[warp] = vi;
+    if (threadIdx.x == 0) sh_wh = 0u;
+    __syncthreads();
+    if (lane == 0 && whead) atomicOr(&sh_wh, 1u << warp);
+    __syncthreads();
+    bool he = false;
+    T ve = T(0);
+    {
+        // exclusive prefix over the warps before this one, in warp order
+        const unsigned wh = sh_wh;
+        for (int w = 0; w < warp; ++w) {
+            bool hw = (wh >> w) & 1u;
+            T vw = sh_wv[w];
+            seg_combine(hw, vw, he, ve);
+            he = hw;
+            ve = vw;
+        }
+        // then the lanes before this one within the warp
+        const bool hl = __shfl_up_sync(0xffffffffu, hi_, 1);
+        const T vl = __shfl_up_sync(0xffffffffu, vi, 1);
+        if (lane > 0) {
+            bool hh = hl;
+            T vv = vl;
+            seg_combine(hh, vv, he, ve);
+            he = hh;
+            ve = vv;
+        }
+    }
+    // running sums: the exclusive carry, then the thread's own positions
+    T r = ve;
+#pragma unroll
+    for (int j = 0; j < kScanIPT; ++j) {
+        r = (hb >> j) & 1u ? x[j] : r + x[j];
+        sh_run[p0 + j] = r;
+    }
+    const bool any_head = __syncthreads_or(h);
+    // publish and look back (warp 0)
+    if (warp == 0) {
+        const T tail = cnt > 0 ? sh_run[cnt - 1] : T(0);
+        if (lane == 0) {
+            if (any_head || !open) {
+                st.inclusive[tile] = tail;
+                __threadfence();
+                *(volatile unsigned*)&st.flag[tile] = 2u;
+            } else {
+                st.aggregate[tile] = tail;
+                __threadfence();
+                *(volatile unsigned*)&st.flag[tile] = 1u;
+            }
+        }
+        T carry = T(0);
+        if (open) {
+            if (!lookback_fold(st, tile, T(0), sh_fold, carry) && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
+            if (lane == 0 && !any_head) {
+                st.inclusive[tile] = carry + tail;
+                __threadfence();
+                *(volatile unsigned*)&st.flag[tile] = 2u;
+            }
+        }
+        if (lane == 0) sh_carry = carry;
+    }
+    __syncthreads();
+    if (open && end_open <= v0 + cnt && threadIdx.x == 0)
+        out[sb - 1] = init + (sh_carry + sh_run[end_open - 1 - v0]);
+    for (int64_t s = sb + threadIdx.x; s < se; s += kScanT) {
+        const int64_t o = offsets[s], e = offsets[s + 1];
+        if (e == o) out[s] = init;
+        else if (e <= v0 + cnt) out[s] = init + sh_run[e - 1 - v0];
+    }
+}
+
+// ---- segmented reduce for offsets that are not a valid partition -------------------
+// One warp per segment, each segment checked on its own: a segment outside
+// [0, n_vals] or with decreasing offsets yields init and is reported.  It runs
+// only when the tile kernel found the offsets invalid (*bad != 0) and then
+// rewrites every output.
 template <class T>
 __global__ void __launch_bounds__(256) segreduce_warp_kernel(const int64_t* __restrict__ offsets, int64_t nseg,
                                                              const T* __restrict__ vals, int64_t n_vals, T init,
-                                                             T* __restrict__ out, unsigned* err) {
+                                                             T* __restrict__ out, const unsigned* invalid,
+                                                             unsigned* err) {
+    if (*(volatile const unsigned*)invalid == 0u) return;
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     bool bad = false;
@@ -349,6 +598,25 @@ extern "C" int hyd_cuda_scan_i64(const int64_t* in, int64_t* out, int64_t n, int
                            reverse != 0, inclusive != 0, as_stream(stream));
 }
 
+// Status scratch of the left-fold look-back for `ntiles` tiles of 8-byte
+// values: [0, 256) the tile counter (+0) and the invalid-offsets word (+4),
+// then the flags, then the aggregates and inclusive values.  The first
+// 256 + 4 * ntiles bytes are zeroed on the stream (one memset).
+template <class T>
+static int fold_status(cudaStream_t s, int64_t ntiles, FoldStatus<T>* st) {
+    const size_t flag_bytes = ((size_t)ntiles * 4 + 255) & ~(size_t)255;
+    void* scratch = nullptr;
+    HYD_TRY(workspace(s, 256 + flag_bytes + 2 * sizeof(T) * (size_t)ntiles, nullptr, &scratch));
+    unsigned char* b = static_cast<unsigned char*>(scratch);
+    st->tile_counter = reinterpret_cast<unsigned*>(b);
+    st->bad = reinterpret_cast<unsigned*>(b + 4);
+    st->flag = reinterpret_cast<unsigned*>(b + 256);
+    st->aggregate = reinterpret_cast<T*>(b + 256 + flag_bytes);
+    st->inclusive = st->aggregate + ntiles;
+    HYD_CUDA_TRY(cudaMemsetAsync(b, 0, 256 + (size_t)ntiles * 4, s));
+    return HYD_CUDA_OK;
+}
+
 extern "C" int hyd_cuda_scan_f64(const double* in, double* out, int64_t n, double init, int reverse,
                                  int inclusive, void* stream) {
     HYD_CHECK_ARG(n >= 0, "scan_f64: negative length");
@@ -357,12 +625,12 @@ extern "C" int hyd_cuda_scan_f64(const double* in, double* out, int64_t n, doubl
     cudaStream_t s = as_stream(stream);
     const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
     HYD_CHECK_ARG(ntiles <= 0x7fffffffLL, "scan_f64: too long");
-    void* scratch = nullptr;
-    HYD_TRY(workspace(s, 8 * (size_t)ntiles, nullptr, &scratch));
-    double* sums = static_cast<double*>(scratch);
-    scan_f64_tile_sums_kernel<<<(unsigned)ntiles, kScanT, 0, s>>>(in, n, reverse != 0, sums);
-    scan_f64_tile_prefix_kernel<<<1, 1024, 0, s>>>(sums, ntiles, init);
-    scan_f64_downsweep_kernel<<<(unsigned)ntiles, kScanT, 0, s>>>(in, out, n, reverse != 0, inclusive != 0, sums);
+    Device* d = nullptr;
+    HYD_TRY(device(&d));
+    FoldStatus<double> st;
+    HYD_TRY(fold_status(s, ntiles, &st));
+    scan_fold_kernel<double><<<(unsigned)ntiles, kScanT, 0, s>>>(in, out, n, init, reverse != 0, inclusive != 0, st,
+                                                                 d->d_err);
     return launch_check("scan_f64");
 }
 
@@ -375,13 +643,21 @@ static int segreduce_launch(const int64_t* offsets, int64_t n_offsets, const T* 
     const int64_t nseg = n_offsets - 1;
     HYD_CHECK_ARG(nseg == 0 || out != nullptr, "%s: null output", what);
     if (nseg == 0) return HYD_CUDA_OK;
+    const int64_t ntiles = n_vals == 0 ? 1 : (n_vals + kScanTile - 1) / kScanTile;
+    HYD_CHECK_ARG(ntiles <= 0x7fffffffLL, "%s: too many values", what);
     Device* d = nullptr;
     HYD_TRY(device(&d));
+    cudaStream_t s = as_stream(stream);
+    FoldStatus<T> st;
+    HYD_TRY(fold_status(s, ntiles, &st));
+    segreduce_tile_kernel<T><<<(unsigned)ntiles, kScanT, 0, s>>>(offsets, nseg, vals, n_vals, init, out, st, ntiles,
+                                                                  d->d_err);
+    HYD_TRY(launch_check(what));
     int64_t blocks = (nseg + 7) / 8;
     const int64_t cap = (int64_t)d->sm_count * 8;
     if (blocks > cap) blocks = cap;
-    segreduce_warp_kernel<T><<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(offsets, nseg, vals, n_vals, init,
-                                                                               out, d->d_err);
+    segreduce_warp_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(offsets, nseg, vals, n_vals, init, out, st.bad,
+                                                              d->d_err);
     return launch_check(what);
 }
 

@@ -55,6 +55,8 @@ SIGNATURES = {
     "hyd_cuda_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i, _p]),
     "hyd_cuda_selftest_dadd": (_i, [_p, _p, _p, _p, _i64, _p]),
     "hyd_cuda_selftest_div": (_i, [_p, _i, _p, _p, _i64, _p]),
+    "hyd_cuda_probe_fp64_rate": (_i, [_i64, _p, C.POINTER(C.c_int64), _p]),
+    "hyd_cuda_selftest_timeout": (_i, [_i, C.c_uint32, _p]),
     "hyd_cuda_iterate_stencil2d_f64_variant": (_i, [_i, _p, _p, _i64, _i64, _i64, _i, C.POINTER(C.c_int), _p]),
     "hyd_cuda_tune_cache_path": (C.c_char_p, []),
     "hyd_cuda_tune_set_cache_path": (_i, [C.c_char_p]),
@@ -579,6 +581,36 @@ def make_array(np_array):
     a = Array(C.pointer(st), np_array.ctypes.data, np_array.itemsize, t)
     a._keep = (st, np_array)
     return a
+
+
+_libc = None
+
+
+def array_free(p):
+    """Release a hyd_array_t* that an export returned, as the reference
+    runtime's hyd_array_free does (runtime/hydrangea_runtime.h:333-343): drop
+    one reference to the storage, free data and storage record at zero, then
+    the header.  The runtime allocates them with malloc/calloc for this."""
+    global _libc
+    if _libc is None:
+        _libc = C.CDLL(None)
+        _libc.free.argtypes = [C.c_void_p]
+    a = p.contents
+    st = a.storage.contents
+    st.refcount -= 1
+    if st.refcount == 0:
+        _libc.free(st.data)
+        _libc.free(C.cast(a.storage, C.c_void_p))
+    _libc.free(C.cast(p, C.c_void_p))
+
+
+def export_weighted_histogram(arr, bins):
+    """hyd_export_weighted_histogram(hyd_array_t*, bins): returns the result as
+    a caller-owned hyd_array_t* (free it with array_free)."""
+    fn = lib().hyd_export_weighted_histogram
+    fn.restype = C.POINTER(Array)
+    fn.argtypes = [C.POINTER(Array), C.c_int64]
+    return fn(C.byref(arr), bins)
 
 
 def weighted_histogram_host(data, bins, strategy=SCATTER_AUTO):

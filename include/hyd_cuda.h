@@ -201,6 +201,22 @@ int hyd_cuda_selftest_dadd(const double* x, const double* y, double* emu, double
  * hw[i] = the IEEE division (round to nearest even).  No counterpart in the
  * reference; for tests. */
 int hyd_cuda_selftest_div(const double* x, int divisor, double* fast, double* hw, int64_t n, void* stream);
+/* Issue-rate probe of the FP64 unit: a kernel of sm_count x 4 blocks of 256
+ * threads, each running `iters` rounds of 8 independent fma chains, so that
+ * the FP64 pipe, not latency, bounds it.  *fma_count (HOST, may be NULL)
+ * receives the number of fma operations launched; the caller times the launch
+ * with CUDA events on `stream` and divides.  sink: two device doubles.  No
+ * counterpart in the reference; it supplies the measured denominator of the
+ * FP64-bound kernels' roofline. */
+int hyd_cuda_probe_fp64_rate(int64_t iters, double* sink, int64_t* fma_count, void* stream);
+/* Timeout self-test: runs one of the runtime's bounded device waits on a
+ * condition that nothing ever satisfies, with at most poll_limit (1..2^20)
+ * polls, so that it gives up.  which = 0: the mbarrier wait of the TMA kernels;
+ * which = 1: the tile-status wait of the decoupled look-back scans.  The wait
+ * sets the device error word exactly as a real timeout does: the next
+ * hyd_cuda_check(stream) returns HYD_CUDA_ERR_TIMEOUT, and the device stays
+ * usable.  No counterpart in the reference; for tests. */
+int hyd_cuda_selftest_timeout(int which, uint32_t poll_limit, void* stream);
 /* ---- fused map / zipwith / generate chains -------------------------------------
  * The element loop of a fused chain (bench/map_chain/map_chain.hyd; the C
  * backend's loop body, CodegenC.hs:1328-1353 for the reduced form) with its

@@ -15,7 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libhyd_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libhyd_refwitness.so")
-DEFAULT_REFERENCE_ROOT = "/root/reference"
+# The reference source tree, read in place: $HYD_REFERENCE_ROOT, else a
+# checkout named ``reference`` beside this repository.
+DEFAULT_REFERENCE_ROOT = os.environ.get(
+    "HYD_REFERENCE_ROOT", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 CFLAGS = ["-O3", "-std=c99", "-fopenmp", "-fPIC", "-shared", "-Wall", "-Wno-unused-function"]
 

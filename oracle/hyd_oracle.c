@@ -127,6 +127,53 @@ double orc_sum_f64_compensated(const double* xs, int64_t n) {
 }
 
 /* ------------------------------------------------------------------------- */
+/* Fused element chains.  Fusion composes map/zipwith/generate chains into one
+ * element function (Fusion.hs:1808-1874: map f (zipwith g xs ys) =>
+ * zipwith (f . g), zipwith f (map g xs) ys => zipwith (\x y -> f (g x) y), ...)
+ * and the C backend emits one `omp parallel for` over the elements with the
+ * composed body (CodegenC.hs:1451-1491), or the reduction template when the
+ * chain ends in reduce (+) (CodegenC.hs:1328-1353).  Two chains are restated:
+ *
+ * bench/map_chain/map_chain.hyd:11-17
+ *   src = generate [n] (fn [i] => float_of i /. float_of n)
+ *   c   = map (x *. 2.0 +. 1.0) (map (x -. 0.5) (map (x *. x) src))
+ *   reduce (+.) 0.0 c
+ * elements: ((s * s) - 0.5) * 2.0 + 1.0 with s = (double)i / (double)n.      */
+static inline double orc_map_chain_elem(int64_t i, int64_t n) {
+    const double s = (double)i / (double)n;
+    const double a = s * s;
+    const double b = a - 0.5;
+    return b * 2.0 + 1.0;
+}
+
+void orc_map_chain_f64(int64_t n, double* out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+        out[i] = orc_map_chain_elem(i, n);
+    }
+}
+
+/* The reduced form as the C backend runs it (reduction template). */
+double orc_map_chain_sum_f64(int64_t n) {
+    double acc = 0.0;
+#pragma omp parallel for simd simdlen(4) reduction(+:acc)
+    for (int64_t i = 0; i < n; i++) {
+        acc = acc + orc_map_chain_elem(i, n);
+    }
+    return acc;
+}
+
+/* zipwith (+.) (zipwith ( *. ) a b) c, fused into one loop over three inputs:
+ * out[i] = a[i] * b[i] + c[i], two IEEE roundings (no contraction).         */
+void orc_zipwith_muladd_f64(const double* a, const double* b, const double* c, double* out, int64_t n) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+        const double p = a[i] * b[i];
+        out[i] = p + c[i];
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* scatter (+) (fill [B] 0) (map (x % B) data) (map (x * x) data).
  * Fusion (scatter re-index, examples/weighted_histogram.hyd:1-25) reads data
  * once per element; Parallelize.hs:466-503 picks the privatized strategy when

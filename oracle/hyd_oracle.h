@@ -29,6 +29,11 @@ double orc_dot_f64_serial(const double* xs, const double* ys, int64_t n);
 double orc_dot_f64_compensated(const double* xs, const double* ys, int64_t n);
 double orc_sum_f64_compensated(const double* xs, int64_t n);
 
+/* ---- fused element chains (map / zipwith / generate) -------------------- */
+void orc_map_chain_f64(int64_t n, double* out);
+double orc_map_chain_sum_f64(int64_t n);
+void orc_zipwith_muladd_f64(const double* a, const double* b, const double* c, double* out, int64_t n);
+
 /* ---- scatter (+) ---------------------------------------------------------- */
 int orc_weighted_hist_i64(const int64_t* data, int64_t n, int64_t bins, int64_t* hist);
 int orc_weighted_hist_i64_atomic(const int64_t* data, int64_t n, int64_t bins, int64_t* hist);

@@ -39,6 +39,9 @@ def lib():
             "orc_dot_f64_serial": (C.c_double, [_f64p, _f64p, _i64]),
             "orc_dot_f64_compensated": (C.c_double, [_f64p, _f64p, _i64]),
             "orc_sum_f64_compensated": (C.c_double, [_f64p, _i64]),
+            "orc_map_chain_f64": (None, [_i64, _f64p]),
+            "orc_map_chain_sum_f64": (C.c_double, [_i64]),
+            "orc_zipwith_muladd_f64": (None, [_f64p, _f64p, _f64p, _f64p, _i64]),
             "orc_weighted_hist_i64": (C.c_int, [_i64p, _i64, _i64, _i64p]),
             "orc_weighted_hist_i64_atomic": (C.c_int, [_i64p, _i64, _i64, _i64p]),
             "orc_hist_generate_i64": (C.c_int, [_i64, _i64, _i64p]),
@@ -141,6 +144,30 @@ def dot_serial(xs, ys):
 
 def dot_compensated(xs, ys):
     return lib().orc_dot_f64_compensated(np.ascontiguousarray(xs), np.ascontiguousarray(ys), len(xs))
+
+
+def sum_compensated(xs):
+    return lib().orc_sum_f64_compensated(np.ascontiguousarray(xs, dtype=np.float64), len(xs))
+
+
+def map_chain(n):
+    """Elements of bench/map_chain/map_chain.hyd's fused chain."""
+    out = np.empty(n, dtype=np.float64)
+    lib().orc_map_chain_f64(n, out)
+    return out
+
+
+def map_chain_sum(n):
+    """The same chain reduced by the C backend's reduction template."""
+    return lib().orc_map_chain_sum_f64(n)
+
+
+def zipwith_muladd(a, b, c):
+    """zipwith (+.) (zipwith ( *. ) a b) c, fused: a*b + c elementwise."""
+    a, b, c = (np.ascontiguousarray(t, dtype=np.float64) for t in (a, b, c))
+    out = np.empty(len(a), dtype=np.float64)
+    lib().orc_zipwith_muladd_f64(a, b, c, out, len(a))
+    return out
 
 
 def weighted_hist(data, bins, atomic=False):

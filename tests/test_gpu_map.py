@@ -1,9 +1,8 @@
 """GPU parity of fused map / zipwith / generate chains compiled at run time
-(hyd_cuda_map_f64): every element bit-identical to the C backend's loop body
-(numpy evaluates the same IEEE operations in the same order, no contraction),
-the (+) reduction within 1e-12 of the compensated sum and identical run to run."""
-import math
-
+(hyd_cuda_map_f64): every element bit-identical to the oracle's restatement of
+the C backend's fused loop (the same IEEE operations in the same order, no
+contraction), the (+) reduction within 1e-12 of the compensated sum and of the
+oracle's reduction template, and identical run to run."""
 import numpy as np
 import pytest
 import torch
@@ -17,28 +16,41 @@ def _map_chain_body(n):
 
 
 @pytest.mark.parametrize("n", [1, 2, 7, 4096, (1 << 20) + 3])
-def test_map_chain_generate_and_reduce(hc, dev, n):
+def test_map_chain_generate_and_reduce(hc, orc, dev, n):
     out = torch.empty(n, dtype=torch.float64, device=dev)
     _, s = hc.map_f64(_map_chain_body(n), [], n=n, out=out, want_sum=True)
-    src = np.arange(n, dtype=np.float64) / float(n)
-    ref = ((src * src) - 0.5) * 2.0 + 1.0
+    ref = orc.map_chain(n)
     assert np.array_equal(out.cpu().numpy().view(np.int64), ref.view(np.int64))
-    exact = math.fsum(ref.tolist())
-    assert abs(s.item() - exact) <= 1e-12 * max(1.0, float(np.abs(ref).sum()))
+    exact = orc.sum_compensated(ref)
+    scale = max(1.0, float(np.abs(ref).sum()))
+    assert abs(s.item() - exact) <= 1e-12 * scale
+    assert abs(s.item() - orc.map_chain_sum(n)) <= 2e-12 * scale
     _, s2 = hc.map_f64(_map_chain_body(n), [], n=n, want_sum=True)  # reduction only, same bits
     assert s2.item() == s.item()
 
 
 @pytest.mark.parametrize("n", [3, 1001, 65536])
 @pytest.mark.parametrize("offset", [0, 1])
-def test_zipwith_three_inputs_elementwise(hc, dev, n, offset):
+def test_zipwith_three_inputs_elementwise(hc, orc, dev, n, offset):
     rng = np.random.default_rng(n + offset)
     host = [rng.uniform(-2, 2, n + 1) for _ in range(3)]
     xs = [torch.from_numpy(h).to(dev)[offset:offset + n] for h in host]
     out = torch.empty(n + 1, dtype=torch.float64, device=dev)[offset:offset + n]
     hc.map_f64("v = x0 * x1 + x2;", xs, out=out)
-    a, b, c = (h[offset:offset + n] for h in host)
-    ref = a * b + c
+    ref = orc.zipwith_muladd(*(h[offset:offset + n] for h in host))
+    assert np.array_equal(out.cpu().numpy().view(np.int64), ref.view(np.int64))
+
+
+def test_zipwith_three_inputs_full_size(hc, orc, dev):
+    """The memory-bound chain of the bench at its full size: 2^27 float64 per
+    input (three inputs and one output, 4 GiB), bit-exact against the oracle."""
+    n = 1 << 27
+    xs = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(3)]
+    for k, t in enumerate(xs):
+        hc.fill_uniform_f64(t, 21 + k, -1.0, 1.0)
+    out = torch.empty(n, dtype=torch.float64, device=dev)
+    hc.map_f64("v = x0 * x1 + x2;", xs, out=out)
+    ref = orc.zipwith_muladd(*(orc.uniform_f64(n, 21 + k, -1.0, 1.0) for k in range(3)))
     assert np.array_equal(out.cpu().numpy().view(np.int64), ref.view(np.int64))
 
 

@@ -103,3 +103,110 @@ def test_segmented_reduce_bad_offsets(hc, dev):
     hc.segmented_reduce(off, vals, out, init=0)
     assert hc.device_check() == hc.ERR_BOUNDS
     assert out.cpu().tolist()[0] == 3
+
+
+def test_scan_f64_many_tiles_deterministic(hc, orc, dev):
+    """The single-pass float64 scan over 2^22 + 77 elements (1025 tiles): within
+    tolerance of the serial fold and bit-identical over repeated runs, whatever
+    order the tiles finished their look-back in."""
+    n = (1 << 22) + 77
+    x = torch.empty(n, dtype=torch.float64, device=dev)
+    hc.fill_uniform_f64(x, 17, -1.0, 1.0)
+    h = x.cpu().numpy()
+    for rev, inc in VARIANTS:
+        outs = []
+        for _ in range(3):
+            out = torch.empty_like(x)
+            hc.scan(x, out, -0.25, rev, inc)
+            outs.append(out)
+        hc.check(hc.device_check())
+        ref = orc.scan_f64(h, -0.25, rev, inc)
+        bound = orc.scan_f64(np.abs(h), 0.25, rev, inc)
+        assert np.all(np.abs(outs[0].cpu().numpy() - ref) <= 1e-12 * np.maximum(bound, 1.0))
+        assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
+
+
+def _segments(rng, nseg, kind):
+    if kind == "loguniform":    # a few segments far longer than a tile, most short
+        lens = np.floor(2.0 ** rng.uniform(0, 20, size=nseg)).astype(np.int64)
+    elif kind == "tile_aligned":  # boundaries on the 4096-value tile edges
+        lens = 4096 * rng.integers(0, 4, size=nseg)
+    elif kind == "one_long":
+        lens = np.ones(nseg, dtype=np.int64)
+        lens[nseg // 2] = 3 * (1 << 20) + 5
+    else:                       # many empty segments between short ones
+        lens = rng.integers(0, 3, size=nseg)
+    return np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+
+
+def _check_segreduce(hc, orc, dev, offsets, nv, seed, init_i=3, init_f=0.25, lead=0):
+    rng = np.random.default_rng(seed)
+    vals_i = rng.integers(-(1 << 40), 1 << 40, size=nv).astype(np.int64)
+    vals_f = rng.uniform(-1, 1, size=nv)
+    nseg = len(offsets) - 1
+    d_off = torch.from_numpy(offsets).to(dev)
+    out_i = torch.empty(nseg, dtype=torch.int64, device=dev)
+    outs_f = [torch.empty(nseg, dtype=torch.float64, device=dev) for _ in range(2)]
+    hc.segmented_reduce(d_off, torch.from_numpy(vals_i).to(dev), out_i, init=init_i)
+    dv = torch.from_numpy(vals_f).to(dev)
+    for o in outs_f:
+        hc.segmented_reduce(d_off, dv, o, init=init_f)
+    hc.check(hc.device_check())
+    assert np.array_equal(out_i.cpu().numpy(), orc.segmented_reduce_i64(offsets, vals_i, init_i))
+    ref = orc.segmented_reduce_f64(offsets, vals_f, init_f)
+    absum = orc.segmented_reduce_f64(offsets, np.abs(vals_f), 0.0)
+    got = outs_f[0].cpu().numpy()
+    assert np.all(np.abs(got - ref) <= 1e-12 * np.maximum(absum, 1.0))
+    assert torch.equal(outs_f[0], outs_f[1])  # run-to-run identical
+
+
+@pytest.mark.parametrize("kind,nseg", [("loguniform", 3000), ("tile_aligned", 700), ("one_long", 20_000),
+                                       ("empty_heavy", 300_000)])
+def test_segmented_reduce_balanced_shapes(hc, orc, dev, kind, nseg):
+    offsets = _segments(np.random.default_rng(nseg), nseg, kind)
+    _check_segreduce(hc, orc, dev, offsets, int(offsets[-1]), seed=nseg)
+
+
+def test_segmented_reduce_values_outside_segments(hc, orc, dev):
+    # offsets[0] > 0 and offsets[-1] < n_vals: the values before the first and
+    # after the last segment belong to none
+    rng = np.random.default_rng(9)
+    lens = rng.integers(0, 9000, size=400)
+    offsets = (5000 + np.concatenate([[0], np.cumsum(lens)])).astype(np.int64)
+    _check_segreduce(hc, orc, dev, offsets, int(offsets[-1]) + 12_345, seed=9)
+
+
+def test_segmented_reduce_empty_values_and_trailing_empties(hc, orc, dev):
+    # no values at all: every segment is empty and yields init
+    _check_segreduce(hc, orc, dev, np.zeros(1001, dtype=np.int64), 0, seed=1)
+    # empty segments at the very end (offset == n_vals) and at a tile edge
+    offsets = np.array([0, 4096, 4096, 4096, 8192, 9000, 9000, 9000], dtype=np.int64)
+    _check_segreduce(hc, orc, dev, offsets, 9000, seed=2)
+
+
+@pytest.mark.parametrize("where", ["middle", "first_negative", "last_beyond"])
+def test_segmented_reduce_invalid_offsets_large(hc, orc, dev, where):
+    """Invalid offsets deep inside a large array: the tiles detect them and the
+    per-segment pass gives every valid segment its sum, every invalid one init,
+    and reports the error."""
+    rng = np.random.default_rng(77)
+    lens = rng.integers(0, 600, size=50_000)
+    offsets = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    nv = int(offsets[-1])
+    if where == "middle":
+        offsets[30_000] = offsets[29_990]      # decreasing pair(s) inside the array
+    elif where == "first_negative":
+        offsets[0] = -3
+    else:
+        offsets[-1] = nv + 10
+    vals = rng.integers(-1000, 1000, size=nv).astype(np.int64)
+    out = torch.empty(len(offsets) - 1, dtype=torch.int64, device=dev)
+    hc.segmented_reduce(torch.from_numpy(offsets).to(dev), torch.from_numpy(vals).to(dev), out, init=7)
+    assert hc.device_check() == hc.ERR_BOUNDS
+    got = out.cpu().numpy()
+    for s in range(len(offsets) - 1):
+        a, b = offsets[s], offsets[s + 1]
+        if a < 0 or b > nv or b < a:
+            assert got[s] == 7, s
+        elif s % 97 == 0 or abs(s - 30_000) < 20:
+            assert got[s] == 7 + int(vals[a:b].sum()), s

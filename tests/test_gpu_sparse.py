@@ -151,6 +151,19 @@ def test_batched_workload_instances_subset(hc, orc, dev):
     _check_batch(hc, orc, desc, rows, cols, vals, x, *out)
 
 
+def test_batched_full_workload_512_instances(hc, orc, dev):
+    """The whole batched workload: 512 instances (seed 4 + i, n = 2^U(10,18),
+    Zipf(1.5) row lengths capped at 256, about 2.9e8 entries) in one batched
+    call, every instance's row_ptr, col_idx and vals bit-exact against the
+    oracle's stable-sort COO -> CSR and y within 1e-12 * sum |v * x| of its
+    sequential row sums."""
+    desc, rows, cols, vals, x = hc.synth_coo_batch(512, seed0=4, min_log2=10, max_log2=18, max_row_len=256)
+    out = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
+    hc.check(hc.device_check())
+    assert int(desc[:, 2].sum()) > 2 * 10**8
+    _check_batch(hc, orc, desc, rows, cols, vals, x, *out)
+
+
 def test_bucketed_and_row_atomic_forms_agree(hc, orc, dev, monkeypatch):
     """Both internal forms of the batched pipeline give identical CSR and y."""
     desc, rows, cols, vals, x = hc.synth_coo_batch(12, seed0=321, min_log2=10, max_log2=15)

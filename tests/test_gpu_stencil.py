@@ -103,6 +103,44 @@ def test_full_size_heat_steps(hc, orc, dev):
     assert np.array_equal(res.cpu().numpy(), orc.iterate_stencil2d(orc.HEAT, init, 4))
 
 
+def _ulp_distance(a, b):
+    """Distance in units in the last place between float64 arrays, through the
+    monotone map of IEEE-754 bit patterns onto the integers."""
+    def ordered(x):
+        i = np.ascontiguousarray(x).view(np.int64)
+        return np.where(i < 0, np.int64(-0x8000000000000000) - i, i)
+    return np.abs(ordered(a) - ordered(b)).astype(np.float64)
+
+
+def test_full_size_heat_1000_steps_drift(hc, orc, dev, record_property):
+    """The heat_2d workload end to end: 8192^2 float64, U[0,1) seed 3, 1000 steps
+    as a captured graph, with the autotuned variant and with the reference's
+    fixed 32x32 tile, against the oracle's 1000-step iterate of the C backend's
+    split-region loops.  The final-state drift is reported in ulp (max, mean);
+    every step is exact, so it must be 0 for both."""
+    h = w = 8192
+    iters = 1000
+    init = _grid(hc, h, w, dev)
+    ref = orc.iterate_stencil2d(orc.HEAT, init.cpu().numpy(), iters)
+    side = torch.cuda.Stream()
+    for name, variant in (("autotuned", -1), ("fixed_32x32", 0)):
+        b0 = init.clone()
+        b1 = torch.empty_like(b0)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            res = hc.iterate_stencil2d(hc.STENCIL_HEAT, b0, b1, iters, stream=side, variant=variant)
+        side.synchronize()
+        hc.check(hc.device_check())
+        got = res.cpu().numpy()
+        d = _ulp_distance(got, ref)
+        record_property("heat_2d_8192_1000_%s_ulp_max" % name, float(d.max()))
+        record_property("heat_2d_8192_1000_%s_ulp_mean" % name, float(d.mean()))
+        print("heat_2d 8192^2 x 1000 steps, %s: drift vs oracle max %g ulp, mean %g ulp"
+              % (name, d.max(), d.mean()))
+        assert d.max() == 0, (name, d.max(), d.mean())
+        del b0, b1, res
+
+
 def test_invalid_arguments(hc, dev):
     g = _grid(hc, 4, 4, dev)
     assert hc.lib().hyd_cuda_stencil2d_f64(7, g.data_ptr(), g.data_ptr(), 4, 4, None) == hc.ERR_INVALID

@@ -317,3 +317,29 @@ def test_guarded_scatter_skips_unguarded_routes(orc):
     guard = np.array([1, 1, 1, 0, 2], np.int64)
     dst, st = orc.scatter_add_guarded_i64(idx, vals, guard, 6)
     assert st == 0 and dst.tolist() == [10, 80, 0, 0, 0, 20]
+
+
+def test_map_chain_restatement(orc):
+    """bench/map_chain/map_chain.hyd: the program text fixes every element
+    (((i/n)^2 - 0.5) * 2 + 1, IEEE operations in order) and the sum has the
+    closed form 2/n^2 * (n-1) n (2n-1) / 6."""
+    for n in (1, 7, 4096, 100003):
+        i = np.arange(n, dtype=np.float64)
+        s = i / float(n)
+        expect = ((s * s) - 0.5) * 2.0 + 1.0
+        got = orc.map_chain(n)
+        assert np.array_equal(got.view(np.int64), expect.view(np.int64))
+        exact = 2.0 * (n - 1) * n * (2 * n - 1) / 6.0 / float(n) / float(n)
+        assert abs(orc.map_chain_sum(n) - exact) <= 1e-12 * max(1.0, exact)
+        assert abs(orc.sum_compensated(got) - exact) <= 1e-13 * max(1.0, exact)
+
+
+def test_zipwith_muladd_restatement(orc):
+    rng = np.random.default_rng(5)
+    a, b, c = (rng.uniform(-3, 3, 10001) for _ in range(3))
+    got = orc.zipwith_muladd(a, b, c)
+    assert np.array_equal(got.view(np.int64), (a * b + c).view(np.int64))
+    # two roundings, not one: differs from a fused multiply-add somewhere
+    fused = np.array([float(np.longdouble(x) * np.longdouble(y) + np.longdouble(z)) for x, y, z in
+                      zip(a[:2000], b[:2000], c[:2000])])
+    assert not np.array_equal(got[:2000], fused) or np.finfo(np.longdouble).nmant <= 52
