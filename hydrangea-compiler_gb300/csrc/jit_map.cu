@@ -25,6 +25,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "hyd_common.cuh"
@@ -70,19 +71,25 @@ static bool load_nvrtc_locked() {
 constexpr int kMapMaxInputs = 8;
 constexpr int kMapThreads = 256;
 
-// Kernel source for `body` over `nin` inputs.
-static std::string map_source(const std::string& body, int nin) {
+// Kernel source for `body` over `nin` inputs of element type T ("double" or
+// "long long").  int64 sums wrap (accumulated as unsigned), as the C backend's
+// int64 arithmetic does on every target it runs on.
+static std::string map_source(const std::string& body, int nin, bool i64) {
+    const std::string T = i64 ? "long long" : "double";
+    const std::string T2 = i64 ? "longlong2" : "double2";
+    const std::string A = i64 ? "unsigned long long" : "double";  // accumulator
+    const std::string zero = i64 ? "0LL" : "0.0";
     std::string s;
-    s += "__device__ __forceinline__ double hyd_elem(long long i";
-    for (int k = 0; k < kMapMaxInputs; ++k) s += ", double x" + std::to_string(k);
-    s += ") {\n  double v = 0.0;\n  (void)i;\n";
+    s += "__device__ __forceinline__ " + T + " hyd_elem(long long i";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += ", " + T + " x" + std::to_string(k);
+    s += ") {\n  " + T + " v = " + zero + ";\n  (void)i;\n";
     for (int k = 0; k < kMapMaxInputs; ++k) s += "  (void)x" + std::to_string(k) + ";\n";
     s += "  {\n" + body + "\n  }\n  return v;\n}\n";
     s += "extern \"C\" __global__ void __launch_bounds__(256) hyd_map_kernel(";
-    for (int k = 0; k < kMapMaxInputs; ++k) s += "const double* __restrict__ p" + std::to_string(k) + ", ";
-    s += "long long n, double* __restrict__ out, double* __restrict__ partials, unsigned int* counter, "
-         "double* __restrict__ sum, int vec) {\n"
-         "  double acc = 0.0;\n"
+    for (int k = 0; k < kMapMaxInputs; ++k) s += "const " + T + "* __restrict__ p" + std::to_string(k) + ", ";
+    s += "long long n, " + T + "* __restrict__ out, " + A + "* __restrict__ partials, unsigned int* counter, " + A +
+         "* __restrict__ sum, int vec) {\n"
+         "  " + A + " acc = 0;\n"
          "  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
          "  const long long nt = (long long)gridDim.x * blockDim.x;\n"
          "  if (vec) {\n"
@@ -91,44 +98,44 @@ static std::string map_source(const std::string& body, int nin) {
          "      const long long i = 2 * q;\n";
     for (int k = 0; k < kMapMaxInputs; ++k) {
         const std::string ks = std::to_string(k);
-        if (k < nin) s += "      const double2 a" + ks + " = ((const double2*)p" + ks + ")[q];\n";
-        else s += "      const double2 a" + ks + " = make_double2(0.0, 0.0);\n";
+        if (k < nin) s += "      const " + T2 + " a" + ks + " = ((const " + T2 + "*)p" + ks + ")[q];\n";
+        else s += "      const " + T2 + " a" + ks + " = {" + zero + ", " + zero + "};\n";
     }
-    s += "      const double v0 = hyd_elem(i";
+    s += "      const " + T + " v0 = hyd_elem(i";
     for (int k = 0; k < kMapMaxInputs; ++k) s += ", a" + std::to_string(k) + ".x";
-    s += ");\n      const double v1 = hyd_elem(i + 1";
+    s += ");\n      const " + T + " v1 = hyd_elem(i + 1";
     for (int k = 0; k < kMapMaxInputs; ++k) s += ", a" + std::to_string(k) + ".y";
     s += ");\n"
-         "      if (out) ((double2*)out)[q] = make_double2(v0, v1);\n"
-         "      acc += v0;\n"
-         "      acc += v1;\n"
+         "      if (out) { " + T2 + " w; w.x = v0; w.y = v1; ((" + T2 + "*)out)[q] = w; }\n"
+         "      acc += (" + A + ")v0;\n"
+         "      acc += (" + A + ")v1;\n"
          "    }\n"
          "    if (t == 0 && (n & 1)) {\n"
          "      const long long i = n - 1;\n"
-         "      const double v = hyd_elem(i";
-    for (int k = 0; k < kMapMaxInputs; ++k) s += k < nin ? ", p" + std::to_string(k) + "[i]" : ", 0.0";
+         "      const " + T + " v = hyd_elem(i";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += k < nin ? ", p" + std::to_string(k) + "[i]" : ", " + zero;
     s += ");\n"
          "      if (out) out[i] = v;\n"
-         "      acc += v;\n"
+         "      acc += (" + A + ")v;\n"
          "    }\n"
          "  } else {\n"
          "    for (long long i = t; i < n; i += nt) {\n"
-         "      const double v = hyd_elem(i";
-    for (int k = 0; k < kMapMaxInputs; ++k) s += k < nin ? ", p" + std::to_string(k) + "[i]" : ", 0.0";
+         "      const " + T + " v = hyd_elem(i";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += k < nin ? ", p" + std::to_string(k) + "[i]" : ", " + zero;
     s += ");\n"
          "      if (out) out[i] = v;\n"
-         "      acc += v;\n"
+         "      acc += (" + A + ")v;\n"
          "    }\n"
          "  }\n"
          "  if (sum == 0) return;\n"
          // fixed shuffle tree per warp, warps in order per block, blocks in order by the last block
-         "  __shared__ double wsum[8];\n"
+         "  __shared__ " + A + " wsum[8];\n"
          "  __shared__ bool last;\n"
          "  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);\n"
          "  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;\n"
          "  __syncthreads();\n"
          "  if (threadIdx.x == 0) {\n"
-         "    double b = 0.0;\n"
+         "    " + A + " b = 0;\n"
          "    for (int w = 0; w < 8; ++w) b += wsum[w];\n"
          "    partials[blockIdx.x] = b;\n"
          "    __threadfence();\n"
@@ -137,7 +144,7 @@ static std::string map_source(const std::string& body, int nin) {
          "  __syncthreads();\n"
          "  if (last && threadIdx.x == 0) {\n"
          "    __threadfence();\n"
-         "    double s = 0.0;\n"
+         "    " + A + " s = 0;\n"
          "    for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(partials + b);\n"
          "    *sum = s;\n"
          "    *counter = 0u;\n"
@@ -150,11 +157,11 @@ struct MapKernel {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t kern = nullptr;
 };
-static std::map<std::tuple<int, int, std::string>, MapKernel> g_map_kernels;
+static std::map<std::tuple<int, int, bool, std::string>, MapKernel> g_map_kernels;
 
-static int compile_map(Device* d, const std::string& body, int nin, MapKernel* out) {
+static int compile_map(Device* d, const std::string& body, int nin, bool i64, MapKernel* out) {
     std::lock_guard<std::mutex> lock(g_jit_mu);
-    auto key = std::make_tuple(d->id, nin, body);
+    auto key = std::make_tuple(d->id, nin, i64, body);
     auto it = g_map_kernels.find(key);
     if (it != g_map_kernels.end()) {
         *out = it->second;
@@ -164,7 +171,7 @@ static int compile_map(Device* d, const std::string& body, int nin, MapKernel* o
     int major = 0, minor = 0;
     HYD_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, d->id));
     HYD_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, d->id));
-    const std::string src = map_source(body, nin);
+    const std::string src = map_source(body, nin, i64);
     nvrtcProgram prog = nullptr;
     if (g_nvrtc.create(&prog, src.c_str(), "hyd_map.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
         return set_error(HYD_CUDA_ERR_CUDA, "map_f64: nvrtcCreateProgram failed");
@@ -206,24 +213,26 @@ void release_map_kernels() {
 
 using namespace hyd;
 
-extern "C" int hyd_cuda_map_f64(const char* body, const double* const* inputs, int ninputs, int64_t n, double* out,
-                                double* sum, void* stream) {
-    HYD_CHECK_ARG(body != nullptr && *body, "map_f64: empty element body");
-    HYD_CHECK_ARG(ninputs >= 0 && ninputs <= kMapMaxInputs, "map_f64: 0..%d inputs", kMapMaxInputs);
-    HYD_CHECK_ARG(n >= 0, "map_f64: negative length");
-    HYD_CHECK_ARG(ninputs == 0 || inputs != nullptr, "map_f64: null input table");
-    for (int k = 0; k < ninputs; ++k) HYD_CHECK_ARG(n == 0 || inputs[k] != nullptr, "map_f64: null input %d", k);
+template <class T>
+static int map_launch(const char* body, const T* const* inputs, int ninputs, int64_t n, T* out, T* sum,
+                      void* stream, const char* what) {
+    HYD_CHECK_ARG(body != nullptr && *body, "%s: empty element body", what);
+    HYD_CHECK_ARG(ninputs >= 0 && ninputs <= kMapMaxInputs, "%s: 0..%d inputs", what, kMapMaxInputs);
+    HYD_CHECK_ARG(n >= 0, "%s: negative length", what);
+    HYD_CHECK_ARG(ninputs == 0 || inputs != nullptr, "%s: null input table", what);
+    for (int k = 0; k < ninputs; ++k) HYD_CHECK_ARG(n == 0 || inputs[k] != nullptr, "%s: null input %d", what, k);
     cudaStream_t s = as_stream(stream);
     Device* d = nullptr;
     HYD_TRY(device(&d));
     MapKernel mk;
-    HYD_TRY(compile_map(d, body, ninputs, &mk));  // compile errors surface even for n == 0
+    // compile errors surface even for n == 0
+    HYD_TRY(compile_map(d, body, ninputs, std::is_integral<T>::value, &mk));
     if (n == 0) {
-        if (sum) HYD_CUDA_TRY(cudaMemsetAsync(sum, 0, sizeof(double), s));
+        if (sum) HYD_CUDA_TRY(cudaMemsetAsync(sum, 0, sizeof(T), s));
         return HYD_CUDA_OK;
     }
     bool vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
-    const double* p[kMapMaxInputs] = {nullptr};
+    const T* p[kMapMaxInputs] = {nullptr};
     for (int k = 0; k < ninputs; ++k) {
         p[k] = inputs[k];
         vec = vec && (reinterpret_cast<uintptr_t>(p[k]) & 15) == 0;
@@ -234,9 +243,9 @@ extern "C" int hyd_cuda_map_f64(const char* body, const double* const* inputs, i
     if (grid > cap) grid = cap;
     unsigned* counters = nullptr;
     void* scratch = nullptr;
-    HYD_TRY(workspace(s, (size_t)grid * sizeof(double), &counters, &scratch));
+    HYD_TRY(workspace(s, (size_t)grid * sizeof(T), &counters, &scratch));
     unsigned* counter = counters + 200;  // reset by the kernel's last block
-    double* partials = static_cast<double*>(scratch);
+    void* partials = scratch;
     long long nn = n;
     int v = vec ? 1 : 0;
     void* args[kMapMaxInputs + 6];
@@ -249,4 +258,16 @@ extern "C" int hyd_cuda_map_f64(const char* body, const double* const* inputs, i
     args[kMapMaxInputs + 5] = &v;
     HYD_CUDA_TRY(cudaLaunchKernel((const void*)mk.kern, dim3((unsigned)grid), dim3(kMapThreads), args, 0, s));
     return HYD_CUDA_OK;
+}
+
+extern "C" int hyd_cuda_map_f64(const char* body, const double* const* inputs, int ninputs, int64_t n, double* out,
+                                double* sum, void* stream) {
+    return map_launch<double>(body, inputs, ninputs, n, out, sum, stream, "map_f64");
+}
+
+extern "C" int hyd_cuda_map_i64(const char* body, const int64_t* const* inputs, int ninputs, int64_t n,
+                                int64_t* out, int64_t* sum, void* stream) {
+    return map_launch<long long>(body, reinterpret_cast<const long long* const*>(inputs), ninputs, n,
+                                 reinterpret_cast<long long*>(out), reinterpret_cast<long long*>(sum), stream,
+                                 "map_i64");
 }

@@ -230,11 +230,17 @@ __device__ __forceinline__ T ld_volatile(const T* p) {
 // is the nearest predecessor that has published an inclusive value (`before`
 // stands for the inclusive value of tile -1).  Every inclusive value is made
 // the same way, so the result is the left fold of all earlier aggregates,
-// whatever the timing.  Aggregates are collected in sbuf (kFoldBuf); when the
-// nearest inclusive predecessor is further back than that, the look-back
-// starts again from tile - 1 (nearer prefixes will have appeared by then).
-// Returns false on every lane when a wait ran out.
-template <class T>
+// whatever the timing.  The fold passes through the inclusive value of every
+// tile s+1 .. tile-1 on the way; with kHelp those are published too: a
+// predecessor still in its own look-back would compute the same bits, so the
+// race is benign, and later tiles find an inclusive value close by (measured:
+// it pays for the segmented reduce, whose tiles without a segment start wait
+// on long chains, and costs the plain scan 10%).
+// Aggregates are collected in sbuf (kFoldBuf); when the nearest inclusive
+// predecessor is further back than that, the look-back starts again from
+// tile - 1 (nearer prefixes will have appeared by then).  Returns false on
+// every lane when a wait ran out.
+template <bool kHelp, class T>
 __device__ bool lookback_fold(const FoldStatus<T>& st, int64_t tile, T before, T* sbuf, T& prefix) {
     const int lane = threadIdx.x & 31;
     unsigned restarts = 0;
@@ -268,8 +274,18 @@ __device__ bool lookback_fold(const FoldStatus<T>& st, int64_t tile, T before, T
     __syncwarp();
     T acc = base;
     if (lane == 0)
-        for (int i = cnt - 1; i >= 0; --i) acc = acc + sbuf[i];
+        for (int i = cnt - 1; i >= 0; --i) {
+            acc = acc + sbuf[i];
+            if (kHelp) sbuf[i] = acc;  // the inclusive value of tile - 1 - i
+        }
     prefix = __shfl_sync(0xffffffffu, acc, 0);
+    if (kHelp) {
+        __syncwarp();
+        for (int i = lane; i < cnt; i += 32) st.inclusive[tile - 1 - i] = sbuf[i];
+        __threadfence();
+        __syncwarp();
+        for (int i = lane; i < cnt; i += 32) *(volatile unsigned*)&st.flag[tile - 1 - i] = 2u;
+    }
     return true;
 }
 
@@ -310,7 +326,8 @@ __global__ void __launch_bounds__(kScanT) scan_fold_kernel(const T* __restrict__
                 *(volatile unsigned*)&st.flag[tile] = 1u;
             }
             T prefix = T(0);
-            if (!lookback_fold(st, tile, init, sh_fold, prefix) && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
+            if (!lookback_fold<false>(st, tile, init, sh_fold, prefix) && lane == 0)
+                raise_error(err, ERRBIT_TIMEOUT);
             if (lane == 0) {
                 st.inclusive[tile] = prefix + agg;
                 __threadfence();
@@ -364,7 +381,7 @@ __device__ __forceinline__ void seg_combine(bool& h, T& v, bool h_before, T v_be
 }
 
 template <class T>
-__global__ void __launch_bounds__(kScanT) segreduce_tile_kernel(const int64_t* __restrict__ offsets, int64_t nseg,
+__global__ void __launch_bounds__(kScanT, 3) segreduce_tile_kernel(const int64_t* __restrict__ offsets, int64_t nseg,
                                                                  const T* __restrict__ vals, int64_t n_vals, T init,
                                                                  T* __restrict__ out, FoldStatus<T> st,
                                                                  int64_t ntiles, unsigned* err) {
@@ -497,7 +514,7 @@ __global__ void __launch_bounds__(kScanT) segreduce_tile_kernel(const int64_t* _
         }
         T carry = T(0);
         if (open) {
-            if (!lookback_fold(st, tile, T(0), sh_fold, carry) && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
+            if (!lookback_fold<true>(st, tile, T(0), sh_fold, carry) && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
             if (lane == 0 && !any_head) {
                 st.inclusive[tile] = carry + tail;
                 __threadfence();

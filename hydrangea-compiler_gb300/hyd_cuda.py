@@ -112,6 +112,7 @@ SIGNATURES = {
     "hyd_cuda_array_device_data": (_p, [_p]),
     "hyd_cuda_array_resident_stats": (_i, [_p, _p, _p]),
     "hyd_cuda_map_f64": (_i, [C.c_char_p, _p, _i, _i64, _p, _p, _p]),
+    "hyd_cuda_map_i64": (_i, [C.c_char_p, _p, _i, _i64, _p, _p, _p]),
     "hyd_cuda_jacobi1d_f64": (_i, [_p, _p, _i64, _p]),
     "hyd_cuda_iterate_jacobi1d_f64": (_i, [_p, _p, _i64, _i64, C.POINTER(C.c_int), _p]),
     "hyd_cuda_gray_scott_step_f64": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _p]),
@@ -319,19 +320,26 @@ def iterate_stencil2d_bnd(kind, boundary, buf0, buf1, iters, fill=0.0, stream=No
     return buf0 if fb.value == 0 else buf1
 
 
-def map_f64(body, inputs, n=None, out=None, want_sum=False, stream=None):
+def map_f64(body, inputs, n=None, out=None, want_sum=False, stream=None, _fn="hyd_cuda_map_f64", _dtype=None):
     """Fused element chain: `body` (C statements assigning v from x0.., i) over
     device tensors `inputs`; returns (out, sum or None)."""
     import torch
+    dtype = torch.float64 if _dtype is None else _dtype
     n = inputs[0].numel() if n is None else n
     table = (C.c_void_p * max(len(inputs), 1))(*[t.data_ptr() for t in inputs])
     s = None
     if want_sum:
         dev = inputs[0].device if inputs else torch.device("cuda")
-        s = torch.zeros(1, dtype=torch.float64, device=dev)
-    call("hyd_cuda_map_f64", body.encode(), C.cast(table, C.c_void_p), len(inputs), n,
+        s = torch.zeros(1, dtype=dtype, device=dev)
+    call(_fn, body.encode(), C.cast(table, C.c_void_p), len(inputs), n,
          ptr(out) if out is not None else None, ptr(s) if s is not None else None, stream_handle(stream))
     return out, s
+
+
+def map_i64(body, inputs, n=None, out=None, want_sum=False, stream=None):
+    """The int64 form of map_f64 (C int64 semantics, wrapping sum)."""
+    import torch
+    return map_f64(body, inputs, n, out, want_sum, stream, _fn="hyd_cuda_map_i64", _dtype=torch.int64)
 
 
 class GrayScott(C.Structure):

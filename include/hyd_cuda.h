@@ -232,6 +232,11 @@ int hyd_cuda_selftest_timeout(int which, uint32_t poll_limit, void* stream);
  * not compile is HYD_CUDA_ERR_INVALID with the compiler's message). */
 int hyd_cuda_map_f64(const char* body, const double* const* inputs, int ninputs, int64_t n, double* out,
                      double* sum, void* stream);
+/* The same for int64 elements (x0..x7, v and the (+) reduction int64): the
+ * generated body keeps C's int64 semantics (truncating / and %); the sum
+ * wraps mod 2^64 and is bit-exact. */
+int hyd_cuda_map_i64(const char* body, const int64_t* const* inputs, int ninputs, int64_t n, int64_t* out,
+                     int64_t* sum, void* stream);
 
 /* ---- the other iterate loops ---------------------------------------------------
  * jacobi_1d (examples/jacobi_1d.hyd:4): out[i] = (in[i-1] + in[i] + in[i+1]) / 3.0
@@ -481,6 +486,39 @@ hyd_array_t* hyd_export_gray_scott(void);
 /* The exports below read an input array from its device-resident copy when
  * the array is attached (next section); otherwise they stream its host data. */
 double hyd_export_dot(hyd_array_t* xs, hyd_array_t* ys);
+
+/* ---- runtime calls of generated host code -----------------------------------
+ * What host code generated for `--backend cuda` calls around the device
+ * primitives, in place of the reference runtime's helpers that the C backend's
+ * generated code calls (runtime/hydrangea_runtime.h: array allocation and
+ * release :292-343, hyd_get_env_int :602-616, the printers that main applies
+ * to each zero-argument procedure :460-536).  They keep the reference's
+ * behaviour: the printers write the same bytes, and a failure is a message on
+ * stderr and exit(1), never a status.  Device work is ordered on the legacy
+ * default stream.
+ *   gen_check      exit(1) with the runtime's message unless status == 0
+ *   gen_alloc      a device buffer (>= 1 byte); gen_free releases it
+ *   gen_zero       zero `bytes` of a device buffer (the `fill [n] 0` of a scatter)
+ *   gen_upload     a new device copy of a host array's data
+ *   gen_download   a new host array (reference layout, refcount 1) of `shape`
+ *                  from a device buffer, after reporting device-detected errors
+ *   gen_read_*     one device scalar, after the same check
+ *   gen_array_free the reference's hyd_array_free
+ *   gen_get_env_int, gen_print_*: the reference's get_env_int and printers */
+void hyd_cuda_gen_check(int status, const char* what);
+void* hyd_cuda_gen_alloc(int64_t bytes);
+void hyd_cuda_gen_free(void* d);
+void hyd_cuda_gen_zero(void* d, int64_t bytes);
+void* hyd_cuda_gen_upload(const hyd_array_t* a);
+hyd_array_t* hyd_cuda_gen_download(const void* d, hyd_tuple_t shape, size_t elem_size);
+int64_t hyd_cuda_gen_read_i64(const int64_t* d);
+double hyd_cuda_gen_read_f64(const double* d);
+void hyd_cuda_gen_array_free(hyd_array_t* a);
+int64_t hyd_cuda_gen_get_env_int(const char* name);
+void hyd_cuda_gen_print_int(int64_t v);
+void hyd_cuda_gen_print_double(double v);
+void hyd_cuda_gen_print_array(const hyd_array_t* a);
+void hyd_cuda_gen_print_float_array(const hyd_array_t* a);
 
 /* ---- the host I/O path: CSV files ------------------------------------------
  * Drop-in forms of the reference runtime's readers and writers

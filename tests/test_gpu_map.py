@@ -66,3 +66,26 @@ def test_body_that_does_not_compile_is_reported(hc, dev):
         hc.map_f64("v = no_such_function(x0);", [x], out=torch.empty_like(x))
     assert e.value.status == hc.ERR_INVALID
     assert "does not compile" in str(e.value)
+
+
+@pytest.mark.parametrize("n", [1, 7, 4096, (1 << 20) + 3])
+def test_map_i64_generate_zipwith_and_sum(hc, orc, dev, n):
+    """int64 chains: generate with C's truncating / and % (the coo_csr_build
+    program's row_of), and zipwith over resident inputs with a wrapping sum."""
+    out = torch.empty(n, dtype=torch.int64, device=dev)
+    body = "long long g = i / 3; v = (g * 17 + 3) - (((g * 17 + 3) / 1000) * 1000);"
+    _, s = hc.map_i64(body, [], n=n, out=out, want_sum=True)
+    g = np.arange(n, dtype=np.int64) // 3
+    ref = (g * 17 + 3) - (((g * 17 + 3) // 1000) * 1000)
+    assert np.array_equal(out.cpu().numpy(), ref)
+    assert s.item() == int(ref.sum())
+    a = torch.empty(n, dtype=torch.int64, device=dev)
+    b = torch.empty(n, dtype=torch.int64, device=dev)
+    hc.fill_uniform_i64(a, 5, 1 << 62)
+    hc.fill_uniform_i64(b, 6, 1 << 62)
+    o2 = torch.empty_like(a)
+    _, s2 = hc.map_i64("v = x0 * 3 + x1;", [a, b], out=o2, want_sum=True)
+    ha, hb = a.cpu().numpy().astype(np.uint64), b.cpu().numpy().astype(np.uint64)
+    ref2 = (ha * np.uint64(3) + hb).astype(np.int64)
+    assert np.array_equal(o2.cpu().numpy(), ref2)
+    assert s2.item() == int(ref2.astype(np.uint64).sum(dtype=np.uint64).astype(np.int64))
