@@ -41,6 +41,8 @@ def test_dot_matches_oracle(hc, orc, dev, n):
     cback = orc.dot(hx, hy) if n else 0.0
     assert abs(got - ref) <= TOL * max(1.0, abs(ref))
     assert abs(cback - ref) <= TOL * max(1.0, abs(ref))
+    # and directly against the C backend's own result (the workload's bound)
+    assert abs(got - cback) <= TOL * max(1.0, abs(cback))
 
 
 def test_dot_full_size_deterministic(hc, orc, dev):
@@ -52,8 +54,11 @@ def test_dot_full_size_deterministic(hc, orc, dev):
         hc.dot_f64(xs, ys, out)
         outs.append(out.item())
     assert outs[0] == outs[1] == outs[2]  # bit-identical run to run
-    ref = orc.dot_compensated(xs.cpu().numpy(), ys.cpu().numpy())
+    hx, hy = xs.cpu().numpy(), ys.cpu().numpy()
+    ref = orc.dot_compensated(hx, hy)
     assert abs(outs[0] - ref) <= TOL * max(1.0, abs(ref))
+    cback = orc.dot(hx, hy)  # the C backend's OpenMP reduction
+    assert abs(outs[0] - cback) <= TOL * max(1.0, abs(cback))
 
 
 def test_dot_unaligned_views(hc, orc, dev):
