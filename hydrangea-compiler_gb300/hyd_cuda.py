@@ -113,6 +113,20 @@ SIGNATURES = {
     "hyd_cuda_array_resident_stats": (_i, [_p, _p, _p]),
     "hyd_cuda_map_f64": (_i, [C.c_char_p, _p, _i, _i64, _p, _p, _p]),
     "hyd_cuda_map_i64": (_i, [C.c_char_p, _p, _i, _i64, _p, _p, _p]),
+    "hyd_cuda_gen_check": (None, [_i, C.c_char_p]),
+    "hyd_cuda_gen_alloc": (_p, [_i64]),
+    "hyd_cuda_gen_free": (None, [_p]),
+    "hyd_cuda_gen_zero": (None, [_p, _i64]),
+    "hyd_cuda_gen_upload": (_p, [_p]),
+    "hyd_cuda_gen_download": (_p, [_p, None, C.c_size_t]),
+    "hyd_cuda_gen_read_i64": (_i64, [_p]),
+    "hyd_cuda_gen_read_f64": (_d, [_p]),
+    "hyd_cuda_gen_array_free": (None, [_p]),
+    "hyd_cuda_gen_get_env_int": (_i64, [C.c_char_p]),
+    "hyd_cuda_gen_print_int": (None, [_i64]),
+    "hyd_cuda_gen_print_double": (None, [_d]),
+    "hyd_cuda_gen_print_array": (None, [_p]),
+    "hyd_cuda_gen_print_float_array": (None, [_p]),
     "hyd_cuda_jacobi1d_f64": (_i, [_p, _p, _i64, _p]),
     "hyd_cuda_iterate_jacobi1d_f64": (_i, [_p, _p, _i64, _i64, C.POINTER(C.c_int), _p]),
     "hyd_cuda_gray_scott_step_f64": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _p]),
