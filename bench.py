@@ -50,6 +50,8 @@ def parse_args():
                    help="heat: run this stencil variant without autotuning (profiling runs)")
     p.add_argument("--instances", type=int, default=512,
                    help="batched: number of COO instances (512 is the configuration; fewer for profiling)")
+    p.add_argument("--n-log2", type=int, default=27,
+                   help="histogram: log2 of the element count (27 is the configuration; smaller for profiling)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-suite", action="store_true",
                    help="skip the other configurations (dot, heat_2d, batched, serving)")
@@ -181,6 +183,8 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
 
+    global N_ELEMS
+    N_ELEMS = 1 << args.n_log2
     data = torch.empty(N_ELEMS, dtype=torch.int64, device=dev)
     hc.fill_uniform_i64(data, SEED, VALUE_BOUND)
     hists = {b: torch.zeros(b, dtype=torch.int64, device=dev) for b in BINS}

@@ -12,7 +12,9 @@
 //  3. split   per tile again: each entry gets its rank inside (tile, bucket)
 //             from a shared-memory atomic, each (tile, bucket) reserves its run
 //             with one global atomic, and the entry is written to the bucket's
-//             region as a 32-bit key (row_in_bucket << 24 | col) plus its value;
+//             region as a 32-bit key (row_in_bucket << 24 | col) plus its value
+//             (the tile's values are prefetched into shared memory with
+//             cp.async while the ranks and reservations are computed);
 //  4. bucket  one CTA per bucket: its entries (at most 2048 in the fast kernel)
 //             are counting-sorted by row into shared memory (64 counters), then
 //             each warp takes rows, sorts a row by column in registers (bitonic
@@ -20,6 +22,9 @@
 //             its SpMV; the row pointers are the shared row offsets.  Buckets
 //             above 2048 entries (64 rows x at most 256) go to an overflow list
 //             handled by a block-wide bitonic sort in 96 KB of shared memory.
+// The work lists of the stages (one item per (instance, tile) and per
+// (instance, bucket)) are written on the device; only the instance table
+// crosses from the host.
 // Requires ncols < 2^24 (24-bit column field) and at most 256 entries per row.
 #include <climits>
 #include <cstring>
@@ -44,6 +49,7 @@ struct BkInst {
     long long nrows, ncols, nnz;
     long long bucket_base;  // first bucket in the batch-wide bucket space
     long long nbuckets;
+    long long tile_base;    // first entry tile in the batch-wide tile list
     long long scan_base;    // entries of all earlier instances
     const int* rows;
     const int* cols;
@@ -115,6 +121,20 @@ __global__ void __launch_bounds__(kBkThreads) bk_count_kernel(const BkInst* __re
     if (bad) raise_error(err, ERRBIT_BOUNDS);
 }
 
+// The work lists of the count/split stages (one item per (instance, entry
+// tile)) and of the bucket stage (one per (instance, bucket)), written on the
+// device: block i writes instance i's items at its tile_base / bucket_base.
+__global__ void bk_items_kernel(const BkInst* __restrict__ inst, int64_t ninst, BkItem* __restrict__ tiles,
+                                BkItem* __restrict__ buckets) {
+    for (int64_t i = blockIdx.x; i < ninst; i += gridDim.x) {
+        const BkInst I = inst[i];
+        const long long nt = (I.nnz + kTileEntries - 1) / kTileEntries;
+        for (long long t = threadIdx.x; t < nt; t += blockDim.x) tiles[I.tile_base + t] = BkItem{(int)i, (int)t};
+        for (long long b = threadIdx.x; b < I.nbuckets; b += blockDim.x)
+            buckets[I.bucket_base + b] = BkItem{(int)i, (int)b};
+    }
+}
+
 __global__ void bk_widen_kernel(const unsigned* __restrict__ c, long long* __restrict__ out, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = c[i];
@@ -122,6 +142,17 @@ __global__ void bk_widen_kernel(const unsigned* __restrict__ c, long long* __res
 
 // Stage 3.
 constexpr int kSplitPer = kTileEntries / kBkThreads;  // 16 entries per thread
+// The tile's values are copied into shared memory with cp.async as soon as
+// the tile starts (8 bytes per copy, each thread the slots it later reads), so
+// no global load is left on the path from the reservations to the stores.
+constexpr size_t kSplitSmem = (size_t)kTileEntries * 8;  // 64 KB of values
+
+__device__ __forceinline__ void cp_async_8(void* smem_dst, const void* gsrc) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(smem_dst)),
+                 "l"(gsrc)
+                 : "memory");
+}
+
 __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* __restrict__ inst,
                                                               const BkItem* __restrict__ items, unsigned nitems,
                                                               unsigned* cursor, const long long* __restrict__ bstart,
@@ -129,17 +160,24 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
                                                               uint4* __restrict__ rec_out, unsigned* err) {
     __shared__ unsigned hist[kMaxSmemBuckets];
     __shared__ unsigned gbase[kMaxSmemBuckets];  // batch-wide slots (< 2^32, checked on the host)
+    extern __shared__ __align__(16) double split_vals[];
     unsigned it;
     bool bad = false;
     while (bk_next(cursor, nitems, it)) {
         const BkItem w = items[it];
         const BkInst I = inst[w.inst];
         const bool smem = I.nbuckets <= kMaxSmemBuckets;
+        const long long t0 = (long long)w.tile * kTileEntries;
+        const long long t1 = t0 + kTileEntries < I.nnz ? t0 + kTileEntries : I.nnz;
+#pragma unroll
+        for (int j = 0; j < kSplitPer; ++j) {
+            const int q = threadIdx.x + j * kBkThreads;
+            if (t0 + q < t1) cp_async_8(split_vals + q, I.vals + t0 + q);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
         if (smem)
             for (int b = threadIdx.x; b < I.nbuckets; b += kBkThreads) hist[b] = 0u;
         __syncthreads();
-        const long long t0 = (long long)w.tile * kTileEntries;
-        const long long t1 = t0 + kTileEntries < I.nnz ? t0 + kTileEntries : I.nnz;
         unsigned key[kSplitPer], rank[kSplitPer];
         int bucket[kSplitPer];
         // the rows and columns of all this thread's entries first (read-only
@@ -184,29 +222,20 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
             }
         }
         __syncthreads();
-        // values in groups of four read-only loads, then their records
-        constexpr int kValGroup = 4;
+        // this thread's values have landed in shared memory (its own copies)
+        asm volatile("cp.async.wait_all;" ::: "memory");
 #pragma unroll
-        for (int j0 = 0; j0 < kSplitPer; j0 += kValGroup) {
-            double v[kValGroup];
-#pragma unroll
-            for (int u = 0; u < kValGroup; ++u) {
-                const long long k = t0 + threadIdx.x + (long long)(j0 + u) * kBkThreads;
-                v[u] = bucket[j0 + u] >= 0 ? __ldg(I.vals + k) : 0.0;
-            }
-#pragma unroll
-            for (int u = 0; u < kValGroup; ++u) {
-                const int j = j0 + u;
-                if (bucket[j] < 0) continue;
-                const long long k = t0 + threadIdx.x + (long long)j * kBkThreads;
-                const long long pos = smem ? (long long)gbase[bucket[j]] + rank[j]
-                                           : bstart[I.bucket_base + bucket[j]] +
-                                                 atomicAdd(&bfill[I.bucket_base + bucket[j]], 1u);
-                // one 16-byte record: the key, the entry's COO position (orders
-                // equal (row, col) keys) and the value
-                rec_out[pos] = make_uint4(key[j], (unsigned)k, (unsigned)__double2loint(v[u]),
-                                          (unsigned)__double2hiint(v[u]));
-            }
+        for (int j = 0; j < kSplitPer; ++j) {
+            if (bucket[j] < 0) continue;
+            const int q = threadIdx.x + j * kBkThreads;
+            const long long k = t0 + q;
+            const double v = split_vals[q];
+            const long long pos = smem ? (long long)gbase[bucket[j]] + rank[j]
+                                       : bstart[I.bucket_base + bucket[j]] +
+                                             atomicAdd(&bfill[I.bucket_base + bucket[j]], 1u);
+            // one 16-byte record: the key, the entry's COO position (orders
+            // equal (row, col) keys) and the value
+            rec_out[pos] = make_uint4(key[j], (unsigned)k, (unsigned)__double2loint(v), (unsigned)__double2hiint(v));
         }
         __syncthreads();
     }
@@ -517,8 +546,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     Device* d = nullptr;
     HYD_TRY(device(&d));
     std::vector<BkInst> inst(bi.size());
-    std::vector<BkItem> tiles, buckets;
-    long long nb_total = 0, entries = 0;
+    long long nb_total = 0, entries = 0, nt_total = 0;
     for (size_t i = 0; i < bi.size(); ++i) {
         const BatchInst& B = bi[i];
         if (B.ncols >= (1LL << 24) || B.nrows >= (1LL << 31)) return HYD_CUDA_ERR_UNSUPPORTED;
@@ -537,15 +565,16 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
         I.csr_cols = B.csr_cols;
         I.csr_vals = B.csr_vals;
         I.y = B.y;
-        for (long long t = 0; t * kTileEntries < B.nnz; ++t) tiles.push_back(BkItem{(int)i, (int)t});
-        for (long long b = 0; b < I.nbuckets; ++b) buckets.push_back(BkItem{(int)i, (int)b});
+        I.tile_base = nt_total;
+        nt_total += (B.nnz + kTileEntries - 1) / kTileEntries;
         nb_total += I.nbuckets;
         entries += B.nnz;
     }
-    if (nb_total >= (1LL << 31) || entries >= (1LL << 32)) return HYD_CUDA_ERR_UNSUPPORTED;
+    if (nb_total >= (1LL << 31) || nt_total >= (1LL << 31) || entries >= (1LL << 32))
+        return HYD_CUDA_ERR_UNSUPPORTED;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t inst_b = al(inst.size() * sizeof(BkInst)), tiles_b = al(tiles.size() * sizeof(BkItem)),
-                 bk_b = al(buckets.size() * sizeof(BkItem));
+    const size_t inst_b = al(inst.size() * sizeof(BkInst)), tiles_b = al((size_t)nt_total * sizeof(BkItem)),
+                 bk_b = al((size_t)nb_total * sizeof(BkItem));
     const size_t cnt_b = al((size_t)nb_total * 4), wide_b = al((size_t)nb_total * 8);
     const size_t vals_b = al((size_t)entries * 8);
     void* buf = nullptr;
@@ -568,39 +597,42 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     uint4* recs = reinterpret_cast<uint4*>(take(2 * vals_b));  // (key, COO position, value) per entry
     BkItem* overflow = reinterpret_cast<BkItem*>(take(bk_b));
     unsigned* cursors = reinterpret_cast<unsigned*>(take(256));
-    const size_t table = inst_b + tiles_b + bk_b;
-    const bool async_tables = staging != nullptr && staging_bytes >= table;
+    // only the instance table crosses from the host; the work lists are
+    // written by bk_items_kernel
+    const bool async_tables = staging != nullptr && staging_bytes >= inst_b;
     if (async_tables) {
-        unsigned char* h = static_cast<unsigned char*>(staging);
-        memcpy(h, inst.data(), inst.size() * sizeof(BkInst));
-        if (!tiles.empty()) memcpy(h + inst_b, tiles.data(), tiles.size() * sizeof(BkItem));
-        memcpy(h + inst_b + tiles_b, buckets.data(), buckets.size() * sizeof(BkItem));
-        HYD_CUDA_TRY(cudaMemcpyAsync(b, h, table, cudaMemcpyHostToDevice, s));
+        memcpy(staging, inst.data(), inst.size() * sizeof(BkInst));
+        HYD_CUDA_TRY(cudaMemcpyAsync(d_inst, staging, inst.size() * sizeof(BkInst), cudaMemcpyHostToDevice, s));
     } else {
         HYD_CUDA_TRY(cudaMemcpyAsync(d_inst, inst.data(), inst.size() * sizeof(BkInst), cudaMemcpyHostToDevice, s));
-        if (!tiles.empty())
-            HYD_CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(BkItem), cudaMemcpyHostToDevice, s));
-        HYD_CUDA_TRY(cudaMemcpyAsync(d_bk, buckets.data(), buckets.size() * sizeof(BkItem), cudaMemcpyHostToDevice, s));
     }
+    {
+        const int64_t ni = (int64_t)inst.size();
+        const unsigned g = (unsigned)(ni < 4096 ? ni : 4096);
+        bk_items_kernel<<<g, 256, 0, s>>>(d_inst, ni, d_tiles, d_bk);
+        HYD_TRY(launch_check("bk_items"));
+    }
+    const size_t n_tiles = (size_t)nt_total, n_buckets = (size_t)nb_total;
     HYD_CUDA_TRY(cudaMemsetAsync(bcount, 0, 2 * cnt_b, s));  // bcount and bfill
     HYD_CUDA_TRY(cudaMemsetAsync(cursors, 0, 64, s));
     const unsigned grid = (unsigned)(d->sm_count * 2);
-    if (!tiles.empty()) {
-        bk_count_kernel<<<grid, kBkThreads, 0, s>>>(d_inst, d_tiles, (unsigned)tiles.size(), cursors + 0, bcount,
+    if (n_tiles) {
+        bk_count_kernel<<<grid, kBkThreads, 0, s>>>(d_inst, d_tiles, (unsigned)n_tiles, cursors + 0, bcount,
                                                     d->d_err);
         HYD_TRY(launch_check("bk_count"));
     }
     bk_widen_kernel<<<grid, 256, 0, s>>>(bcount, wide, nb_total);
     HYD_TRY(launch_check("bk_widen"));
     HYD_TRY(scan_i64_launch(wide, bstart, nb_total, 0, false, false, s));
-    if (!tiles.empty()) {
-        bk_split_kernel<<<grid, kBkThreads, 0, s>>>(d_inst, d_tiles, (unsigned)tiles.size(), cursors + 1, bstart,
-                                                    bfill, recs, d->d_err);
+    if (n_tiles) {
+        HYD_TRY(configure_kernel((const void*)bk_split_kernel, d, false));
+        bk_split_kernel<<<grid, kBkThreads, kSplitSmem, s>>>(d_inst, d_tiles, (unsigned)n_tiles, cursors + 1, bstart,
+                                                             bfill, recs, d->d_err);
         HYD_TRY(launch_check("bk_split"));
     }
     HYD_TRY(configure_kernel((const void*)bk_bucket_small_kernel, d, false));
     bk_bucket_small_kernel<<<(unsigned)(d->sm_count * kBkSmallPerSm), kBkSmallThreads, kBkSmallSmem, s>>>(
-        d_inst, d_bk, (unsigned)buckets.size(), cursors + 2, bstart, bcount, recs, overflow, cursors + 4, d->d_err);
+        d_inst, d_bk, (unsigned)n_buckets, cursors + 2, bstart, bcount, recs, overflow, cursors + 4, d->d_err);
     HYD_TRY(launch_check("bk_bucket_small"));
     HYD_TRY(configure_kernel((const void*)bk_bucket_kernel, d, false));
     bk_bucket_kernel<<<grid, kBkThreads, kBkSmem, s>>>(d_inst, overflow, cursors + 4, cursors + 3, bstart, bcount,
@@ -611,13 +643,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
 }
 
 size_t batch_pipeline_bucketed_table_bytes(const std::vector<BatchInst>& bi) {
-    size_t tiles = 0, buckets = 0;
-    for (const BatchInst& B : bi) {
-        tiles += (size_t)((B.nnz + kTileEntries - 1) / kTileEntries);
-        buckets += (size_t)((B.nrows + kBkRows - 1) / kBkRows);
-    }
-    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    return al(bi.size() * sizeof(BkInst)) + al(tiles * sizeof(BkItem)) + al(buckets * sizeof(BkItem));
+    return (bi.size() * sizeof(BkInst) + 255) & ~(size_t)255;
 }
 
 }  // namespace hyd
