@@ -268,10 +268,13 @@ __device__ __forceinline__ void warp_bitonic_sort(K (&key)[kPer], double (&val)[
 
 // Sort key: column, then COO position -- the runtime's stable order for equal
 // (row, col) entries.
+// Columns are bounded by ncols before x is read: with invalid entries in the
+// batch (reported by stage 1) a row can include a slot that no entry wrote,
+// and whatever it holds must not index x.
 template <int kPer>
 __device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* __restrict__ cv,
                                                   const unsigned* __restrict__ coo_idx, int len,
-                                                  const double* __restrict__ x, double* yrow) {
+                                                  const double* __restrict__ x, long long ncols, double* yrow) {
     const int lane = threadIdx.x & 31;
     long long key[kPer];
     double val[kPer];
@@ -290,7 +293,7 @@ __device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* 
             const int c = (int)(key[j] >> 32);
             cc[i] = c;
             cv[i] = val[j];
-            acc = fma(val[j], x[c], acc);
+            acc = fma(val[j], (unsigned)c < (unsigned long long)ncols ? x[c] : 0.0, acc);
         }
     }
     if (len <= 32) {
@@ -299,7 +302,8 @@ __device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* 
         for (int i = 0; i < len; ++i) {
             const long long k = __shfl_sync(0xffffffffu, key[0], i);
             const double v = __shfl_sync(0xffffffffu, val[0], i);
-            acc = fma(v, x[(int)(k >> 32)], acc);
+            const int c = (int)(k >> 32);
+            acc = fma(v, (unsigned)c < (unsigned long long)ncols ? x[c] : 0.0, acc);
         }
         if (lane == 0) *yrow = acc;
         return;
@@ -325,8 +329,12 @@ __global__ void __launch_bounds__(kBatchThreads) batch_sort_spmv_kernel(
         const long long r1 = r0 + kRowTile < I.nrows ? r0 + kRowTile : I.nrows;
         for (long long r = r0 + warp; r < r1; r += W) {
             const long long g = I.row_base + r;
-            const long long s = row_start[g] - I.scan_base;
-            const long long e = (r + 1 < I.nrows) ? row_start[g + 1] - I.scan_base : I.nnz;
+            long long s = row_start[g] - I.scan_base;
+            long long e = (r + 1 < I.nrows) ? row_start[g + 1] - I.scan_base : I.nnz;
+            // with invalid entries (reported by stage 1) the counts and the
+            // instance's extent disagree: keep the span inside the instance
+            s = s < 0 ? 0 : (s > I.nnz ? I.nnz : s);
+            e = e < s ? s : (e > I.nnz ? I.nnz : e);
             const int len = (int)(e - s);
             if (lane == 0) {
                 I.row_ptr[r] = s;
@@ -335,10 +343,10 @@ __global__ void __launch_bounds__(kBatchThreads) batch_sort_spmv_kernel(
             int* cc = I.csr_cols + s;
             double* cv = I.csr_vals + s;
             const unsigned* ci = coo_idx + I.scan_base + s;
-            if (len <= 32) sort_row_and_spmv<1>(cc, cv, ci, len, I.x, I.y + r);
-            else if (len <= 64) sort_row_and_spmv<2>(cc, cv, ci, len, I.x, I.y + r);
-            else if (len <= 128) sort_row_and_spmv<4>(cc, cv, ci, len, I.x, I.y + r);
-            else if (len <= 256) sort_row_and_spmv<8>(cc, cv, ci, len, I.x, I.y + r);
+            if (len <= 32) sort_row_and_spmv<1>(cc, cv, ci, len, I.x, I.ncols, I.y + r);
+            else if (len <= 64) sort_row_and_spmv<2>(cc, cv, ci, len, I.x, I.ncols, I.y + r);
+            else if (len <= 128) sort_row_and_spmv<4>(cc, cv, ci, len, I.x, I.ncols, I.y + r);
+            else if (len <= 256) sort_row_and_spmv<8>(cc, cv, ci, len, I.x, I.ncols, I.y + r);
             else bad = true;  // rows above 256 entries are outside this kernel's contract
         }
     }

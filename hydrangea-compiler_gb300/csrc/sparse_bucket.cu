@@ -250,6 +250,11 @@ constexpr int kBkRounds = kBkSmallCap / kBkSmallThreads;  // 32-element rounds p
 // two (key, index) buffers, per-(warp, digit) counts, digit bases
 constexpr size_t kBkSmallSmem = (size_t)kBkSmallCap * 12 + (size_t)kBkSmallWarps * 256 * 4 + 256 * 4;
 
+// With invalid entries in a batch (reported by the count and split stages) a
+// bucket's count can include an entry whose record the split did not write
+// (a valid row with an invalid column): every column is bounded by ncols
+// before x is read, so such a slot cannot index outside x.
+//
 // Equal (row, col) keys must keep their COO order (the runtime's stable
 // sort_indices).  The split's order inside a bucket is arbitrary, so after the
 // sort every run of equal keys is put in COO-position order (insertion sort
@@ -422,7 +427,10 @@ __global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_smal
                 const int a = (int)dbase[r], bb = row_end(r);
                 if (bb - a <= 32) {
                     double acc = 0.0;
-                    for (int p = a; p < bb; ++p) acc = fma(bk_rec_val(rec_in[s0 + iin[p]]), I.x[kin[p] & cmask], acc);
+                    for (int p = a; p < bb; ++p) {
+                        const unsigned c = kin[p] & cmask;
+                        acc = fma(bk_rec_val(rec_in[s0 + iin[p]]), c < I.ncols ? I.x[c] : 0.0, acc);
+                    }
                     I.y[r0 + r] = acc;
                 }
             }
@@ -432,8 +440,10 @@ __global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_smal
             if (bb - a <= 32) continue;  // warp-uniform
             if (bb - a > 256) bad = true;  // a row above 256 entries: outside the contract
             double acc = 0.0;
-            for (int p = a + lane; p < bb; p += 32)
-                acc = fma(bk_rec_val(rec_in[s0 + iin[p]]), I.x[kin[p] & cmask], acc);
+            for (int p = a + lane; p < bb; p += 32) {
+                const unsigned c = kin[p] & cmask;
+                acc = fma(bk_rec_val(rec_in[s0 + iin[p]]), c < I.ncols ? I.x[c] : 0.0, acc);
+            }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) I.y[r0 + r] = acc;
@@ -520,16 +530,20 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
             const int r = warp * 32 + lane;
             if (r < nr && rstart[r + 1] - rstart[r] <= 32) {
                 double acc = 0.0;
-                for (int p = rstart[r]; p < rstart[r + 1]; ++p)
-                    acc = fma(bk_rec_val(rec_in[s0 + idx[p]]), I.x[key[p] & 0xFFFFFFu], acc);
+                for (int p = rstart[r]; p < rstart[r + 1]; ++p) {
+                    const unsigned c = key[p] & 0xFFFFFFu;
+                    acc = fma(bk_rec_val(rec_in[s0 + idx[p]]), c < I.ncols ? I.x[c] : 0.0, acc);
+                }
                 I.y[r0 + r] = acc;
             }
         }
         for (int r = warp; r < nr; r += kBkThreads / 32) {
             if (rstart[r + 1] - rstart[r] <= 32) continue;  // warp-uniform
             double acc = 0.0;
-            for (int p = rstart[r] + lane; p < rstart[r + 1]; p += 32)
-                acc = fma(bk_rec_val(rec_in[s0 + idx[p]]), I.x[key[p] & 0xFFFFFFu], acc);
+            for (int p = rstart[r] + lane; p < rstart[r + 1]; p += 32) {
+                const unsigned c = key[p] & 0xFFFFFFu;
+                acc = fma(bk_rec_val(rec_in[s0 + idx[p]]), c < I.ncols ? I.x[c] : 0.0, acc);
+            }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) I.y[r0 + r] = acc;

@@ -507,10 +507,11 @@ def batched_coo_csr_spmv(desc, rows, cols, vals, x, stream=None):
     nnz = int(desc[:, 2].sum())
     nr = int(desc[:, 0].sum())
     dev = x.device
-    row_ptr = torch.zeros(nr + ninst, dtype=torch.int64, device=dev)
-    csr_cols = torch.zeros(max(nnz, 1), dtype=torch.int32, device=dev)
-    csr_vals = torch.zeros(max(nnz, 1), dtype=torch.float64, device=dev)
-    y = torch.zeros(nr, dtype=torch.float64, device=dev)
+    # every element is written by the pipeline: no fill kernels
+    row_ptr = torch.empty(nr + ninst, dtype=torch.int64, device=dev)
+    csr_cols = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    csr_vals = torch.empty(max(nnz, 1), dtype=torch.float64, device=dev)
+    y = torch.empty(nr, dtype=torch.float64, device=dev)
     call("hyd_cuda_batched_coo_csr_spmv_f64", ninst, desc.ctypes.data, ptr(rows), ptr(cols), ptr(vals), ptr(x),
          ptr(row_ptr), ptr(csr_cols), ptr(csr_vals), ptr(y), stream_handle(stream))
     return row_ptr, csr_cols, csr_vals, y
