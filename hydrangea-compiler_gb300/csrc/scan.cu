@@ -46,6 +46,7 @@ namespace hyd {
 constexpr int kScanT = 512;
 constexpr int kScanIPT = 8;
 constexpr int kScanTile = kScanT * kScanIPT;  // 4096 (32 KiB of static shared memory for int64)
+constexpr int kScanCtasPerSm = 4;  // resident CTAs per SM (32 registers per thread)
 
 // --- block-wide exclusive scan of one value per thread (int64, wrapping) ------
 template <class T>
@@ -120,7 +121,7 @@ struct ScanStatus {
 
 __device__ __forceinline__ long long ld_volatile_i64(const long long* p) { return *(volatile const long long*)p; }
 
-__global__ void __launch_bounds__(kScanT) scan_i64_lookback_kernel(const long long* __restrict__ in,
+__global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_i64_lookback_kernel(const long long* __restrict__ in,
                                                                     long long* __restrict__ out, int64_t n,
                                                                     long long init, bool reverse,
                                                                     bool inclusive, ScanStatus st,
@@ -291,7 +292,7 @@ __device__ bool lookback_fold(const FoldStatus<T>& st, int64_t tile, T before, T
 
 // float64 (and any T) scan with the left-fold look-back.
 template <class T>
-__global__ void __launch_bounds__(kScanT) scan_fold_kernel(const T* __restrict__ in, T* __restrict__ out, int64_t n,
+__global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_fold_kernel(const T* __restrict__ in, T* __restrict__ out, int64_t n,
                                                             T init, bool reverse, bool inclusive, FoldStatus<T> st,
                                                             unsigned* err) {
     __shared__ T sh_tile[kScanTile];
@@ -381,7 +382,7 @@ __device__ __forceinline__ void seg_combine(bool& h, T& v, bool h_before, T v_be
 }
 
 template <class T>
-__global__ void __launch_bounds__(kScanT, 3) segreduce_tile_kernel(const int64_t* __restrict__ offsets, int64_t nseg,
+__global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(const int64_t* __restrict__ offsets, int64_t nseg,
                                                                  const T* __restrict__ vals, int64_t n_vals, T init,
                                                                  T* __restrict__ out, FoldStatus<T> st,
                                                                  int64_t ntiles, unsigned* err) {
