@@ -27,7 +27,7 @@
 //    slot (instance ranges are contiguous, so this is also each instance's
 //    row_ptr shifted by its entry base), (3) scatter every entry into its row
 //    (atomic slot within the row), (4) per row: sort by column and compute that
-//    row's SpMV in the same warp.  Columns are unique within a row in this
+//    row's SpMV (one fma chain in column order) in the same warp.  Columns are unique within a row in this
 //    workload, so sorting fixes the in-row order and the CSR is bit-exact
 //    however the atomics interleaved.
 #include <cstdlib>
@@ -137,13 +137,6 @@ static int spmv_dispatch(int g, int64_t nrows, const long long* row_ptr, const C
         default: spmv_csr_kernel<32, C><<<(unsigned)blocks, 256, 0, stream>>>(nrows, row_ptr, col_idx, vals, x, ncols, y, d->d_err); break;
     }
     return launch_check("spmv_csr");
-}
-
-// Lanes per row from the average row length (power of two, 1..32).
-static int lanes_for(double avg) {
-    int g = 1;
-    while (g < 32 && g < avg) g <<= 1;
-    return g;
 }
 
 // ---------------------------------------------------------------- batched pipeline
@@ -285,31 +278,26 @@ __device__ __forceinline__ void sort_row_and_spmv(int* __restrict__ cc, double* 
         val[j] = i < len ? cv[i] : 0.0;
     }
     warp_bitonic_sort<kPer>(key, val);
-    double acc = 0.0;
+    double xv[kPer];
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
         const int i = j * 32 + lane;
+        xv[j] = 0.0;
         if (i < len) {
             const int c = (int)(key[j] >> 32);
             cc[i] = c;
             cv[i] = val[j];
-            acc = fma(val[j], (unsigned)c < (unsigned long long)ncols ? x[c] : 0.0, acc);
+            if ((unsigned)c < (unsigned long long)ncols) xv[j] = x[c];
         }
     }
-    if (len <= 32) {
-        // the bucketed form's order for short rows: one sum in column order
-        acc = 0.0;
-        for (int i = 0; i < len; ++i) {
-            const long long k = __shfl_sync(0xffffffffu, key[0], i);
-            const double v = __shfl_sync(0xffffffffu, val[0], i);
-            const int c = (int)(k >> 32);
-            acc = fma(v, (unsigned)c < (unsigned long long)ncols ? x[c] : 0.0, acc);
-        }
-        if (lane == 0) *yrow = acc;
-        return;
-    }
+    // y: one fma chain over the row in column order (position i sits on lane
+    // i % 32, register i / 32), the order of the bucketed form
+    double acc = 0.0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    for (int j = 0; j < kPer; ++j) {
+        for (int l = 0; l < 32 && j * 32 + l < len; ++l)
+            acc = fma(__shfl_sync(0xffffffffu, val[j], l), __shfl_sync(0xffffffffu, xv[j], l), acc);
+    }
     if (lane == 0) *yrow = acc;
 }
 

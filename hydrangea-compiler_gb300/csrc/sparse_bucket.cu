@@ -15,16 +15,17 @@
 //             region as a 32-bit key (row_in_bucket << 24 | col) plus its value
 //             (the tile's values are prefetched into shared memory with
 //             cp.async while the ranks and reservations are computed);
-//  4. bucket  one CTA per bucket: its entries (at most 2048 in the fast kernel)
-//             are counting-sorted by row into shared memory (64 counters), then
-//             each warp takes rows, sorts a row by column in registers (bitonic
-//             network over shuffles), writes its CSR columns/values and computes
-//             its SpMV; the row pointers are the shared row offsets.  Buckets
-//             above 2048 entries (64 rows x at most 256) go to an overflow list
-//             handled by a block-wide bitonic sort in 96 KB of shared memory.
-// The work lists of the stages (one item per (instance, tile) and per
-// (instance, bucket)) are written on the device; only the instance table
-// crosses from the host.
+//  4. bucket  one warp per bucket (at most 2048 entries, ncols <= 2^18): a
+//             stable LSD radix sort of the packed (row, col) keys in shared
+//             memory, the CSR columns/values written in sorted order and the
+//             row pointers from the row changes.  Larger buckets go to an
+//             overflow list sorted by a block-wide bitonic network;
+//  5. spmv    one warp per 256-row chunk of an instance: the rows are ordered
+//             by length in shared memory and each lane sums one row's fma
+//             chain in column order, 32 rows of similar length at a time.
+// The work lists of the stages (one item per (instance, tile), per (instance,
+// bucket) and per (instance, 256-row chunk)) are written on the device; only
+// the instance table crosses from the host.
 // Requires ncols < 2^24 (24-bit column field) and at most 256 entries per row.
 #include <climits>
 #include <cstring>
@@ -50,6 +51,7 @@ struct BkInst {
     long long bucket_base;  // first bucket in the batch-wide bucket space
     long long nbuckets;
     long long tile_base;    // first entry tile in the batch-wide tile list
+    long long chunk_base;   // first 256-row SpMV chunk in the batch-wide chunk list
     long long scan_base;    // entries of all earlier instances
     const int* rows;
     const int* cols;
@@ -121,17 +123,22 @@ __global__ void __launch_bounds__(kBkThreads) bk_count_kernel(const BkInst* __re
     if (bad) raise_error(err, ERRBIT_BOUNDS);
 }
 
+constexpr int kSpRows = 256;  // rows per SpMV chunk
+
 // The work lists of the count/split stages (one item per (instance, entry
-// tile)) and of the bucket stage (one per (instance, bucket)), written on the
-// device: block i writes instance i's items at its tile_base / bucket_base.
+// tile)), of the bucket stage (one per (instance, bucket)) and of the SpMV
+// (one per (instance, 256-row chunk)), written on the device: block i writes
+// instance i's items at its tile_base / bucket_base / chunk_base.
 __global__ void bk_items_kernel(const BkInst* __restrict__ inst, int64_t ninst, BkItem* __restrict__ tiles,
-                                BkItem* __restrict__ buckets) {
+                                BkItem* __restrict__ buckets, BkItem* __restrict__ chunks) {
     for (int64_t i = blockIdx.x; i < ninst; i += gridDim.x) {
         const BkInst I = inst[i];
         const long long nt = (I.nnz + kTileEntries - 1) / kTileEntries;
+        const long long nc = (I.nrows + kSpRows - 1) / kSpRows;
         for (long long t = threadIdx.x; t < nt; t += blockDim.x) tiles[I.tile_base + t] = BkItem{(int)i, (int)t};
         for (long long b = threadIdx.x; b < I.nbuckets; b += blockDim.x)
             buckets[I.bucket_base + b] = BkItem{(int)i, (int)b};
+        for (long long c = threadIdx.x; c < nc; c += blockDim.x) chunks[I.chunk_base + c] = BkItem{(int)i, (int)c};
     }
 }
 
@@ -243,13 +250,6 @@ __global__ void __launch_bounds__(kBkThreads, 2) bk_split_kernel(const BkInst* _
 }
 
 // ---- stage 4 ------------------------------------------------------------------
-constexpr int kBkSmallThreads = 256;
-constexpr int kBkSmallWarps = kBkSmallThreads / 32;
-constexpr int kBkSmallCap = 2048;  // entries of a bucket handled in the fast kernel
-constexpr int kBkRounds = kBkSmallCap / kBkSmallThreads;  // 32-element rounds per warp
-// two (key, index) buffers, per-(warp, digit) counts, digit bases
-constexpr size_t kBkSmallSmem = (size_t)kBkSmallCap * 12 + (size_t)kBkSmallWarps * 256 * 4 + 256 * 4;
-
 // With invalid entries in a batch (reported by the count and split stages) a
 // bucket's count can include an entry whose record the split did not write
 // (a valid row with an invalid column): every column is bounded by ncols
@@ -281,176 +281,194 @@ __device__ __forceinline__ void bk_order_equal_keys(const unsigned* key, IdxT* p
     }
 }
 
-// Fast path: a stable LSD radix sort of the bucket's keys (row_in_bucket <<
-// cbits | col, 6 + cbits bits, 8 per pass) in shared memory; each warp owns
-// consecutive positions, ranked in rounds of 32 with __match_any_sync so equal
-// digits keep their order.  Row starts come from the row changes of the sorted
-// keys.  Then CSR columns/values are written in sorted
-// order (values gathered by index), and each warp computes the SpMV of its
-// rows with lane i summing sorted positions i, i+32, ... (the same order as the
-// other kernels).  Buckets above kBkSmallCap go to `overflow`.
-constexpr int kBkSmallPerSm = 6;  // resident CTAs per SM
-__global__ void __launch_bounds__(kBkSmallThreads, kBkSmallPerSm) bk_bucket_small_kernel(
+// One warp per bucket: a warp sorts its own bucket with no block barrier, so
+// twelve independent buckets are in flight per SM.  (A CTA per ~800-entry
+// bucket pays its fixed work -- zeroing and scanning a counter set per warp,
+// five block barriers per radix pass -- once per bucket.)
+//  * key24 = row_in_bucket << cbits | col, kept to its 6 + cbits <= 24 bits,
+//    sorted by stable LSD passes of 8 bits (at most three);
+//  * the digit counts of every pass are taken in one sweep when the keys are
+//    loaded (the multiset of digits does not change between passes), as
+//    16-bit counts packed two to a word (digits d and d + 128);
+//  * pass 0 reads key24 with the implicit index = position and writes
+//    (key24 >> 8) << 11 | index; later passes move that word, whose bits
+//    8k + 3 ... hold digit k, so one 32-bit word per entry carries both the
+//    remaining key and the entry index;
+//  * each pass ranks 32 positions per round with __match_any_sync, so equal
+//    digits keep their order;
+//  * after the sort every slot's record is gathered once for its full key,
+//    CSR column and value; runs of equal keys are then put in COO order.
+// Row starts come from the masked keys, which are sorted on every bit they
+// have whatever the records hold, so every row range stays inside [0, E].
+// Buckets above kBkWarpCap entries, or of instances with more than 2^18
+// columns, go to `overflow` (the block-wide kernel below).
+constexpr int kBkWarpCap = 2048;
+constexpr int kBkWarpIdxBits = 11;  // log2(kBkWarpCap)
+constexpr int kBkWarpMaxCbits = 24 - kBkShift;
+constexpr int kBkWarpWarps = 4;  // warps (buckets) per CTA
+constexpr int kBkWarpPerSm = 3;  // resident CTAs per SM
+// per warp (32-bit words): two key buffers, packed digit counts of three
+// passes, the running digit bases (later the row starts)
+constexpr int kBkWarpWords = 2 * kBkWarpCap + 3 * 128 + 256;
+constexpr size_t kBkWarpSmem = (size_t)kBkWarpWarps * kBkWarpWords * 4;
+
+// The sort key of a record: row_in_bucket << cbits | col, kept to its 6 + cbits
+// bits (which change nothing for a valid entry, and keep every key's row
+// below kBkRows whatever an unwritten slot holds).
+__device__ __forceinline__ unsigned bk_key24(unsigned k, int cbits) {
+    return (((k >> 24) << cbits) | (k & 0xFFFFFFu)) & ((1u << (kBkShift + cbits)) - 1u);
+}
+
+__global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_warp_kernel(
     const BkInst* __restrict__ inst, const BkItem* __restrict__ items, unsigned nitems, unsigned* cursor,
     const long long* __restrict__ bstart, const unsigned* __restrict__ bcount, const uint4* __restrict__ rec_in,
     BkItem* __restrict__ overflow, unsigned* overflow_count, unsigned* err) {
-    extern __shared__ __align__(16) unsigned char bks_smem[];
-    unsigned* kbuf0 = reinterpret_cast<unsigned*>(bks_smem);
-    unsigned* kbuf1 = kbuf0 + kBkSmallCap;
-    unsigned short* ibuf0 = reinterpret_cast<unsigned short*>(kbuf1 + kBkSmallCap);
-    unsigned short* ibuf1 = ibuf0 + kBkSmallCap;
-    unsigned* wcount = reinterpret_cast<unsigned*>(ibuf1 + kBkSmallCap);  // [warps][256]
-    unsigned* dbase = wcount + kBkSmallWarps * 256;                        // [256]
+    extern __shared__ __align__(16) unsigned bkw_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned* const a = bkw_smem + (size_t)warp * kBkWarpWords;
+    unsigned* const b = a + kBkWarpCap;
+    unsigned* const hist = b + kBkWarpCap;  // [3][128]
+    unsigned* const base = hist + 3 * 128;  // [256]; row starts [65] after the sort
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-    unsigned it;
-    bool bad = false;
-    while (bk_next(cursor, nitems, it)) {
+    for (;;) {
+        unsigned it = 0;
+        if (lane == 0) it = atomicAdd(cursor, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= nitems) break;
         const BkItem w = items[it];
         const BkInst I = inst[w.inst];
         const long long gb = I.bucket_base + w.tile;
         const int E = (int)bcount[gb];
-        if (E > kBkSmallCap) {
-            if (threadIdx.x == 0) overflow[atomicAdd(overflow_count, 1u)] = w;
-            continue;  // uniform
+        int cbits = 0;
+        while ((1LL << cbits) < I.ncols) ++cbits;
+        if (E > kBkWarpCap || cbits > kBkWarpMaxCbits) {
+            if (lane == 0) overflow[atomicAdd(overflow_count, 1u)] = w;
+            continue;  // warp-uniform
         }
         const long long s0 = bstart[gb];
         const long long e0 = s0 - I.scan_base;
         const long long r0 = (long long)w.tile << kBkShift;
         const int nr = (int)((I.nrows - r0) < kBkRows ? (I.nrows - r0) : kBkRows);
-        int cbits = 0;
-        while ((1LL << cbits) < I.ncols) ++cbits;
-        // key = row_in_bucket << cbits | col: 6 + cbits bits, 8 per pass
-        const int passes = (kBkShift + cbits + 7) / 8;
-        for (int i = threadIdx.x; i < E; i += kBkSmallThreads) {
-            const unsigned k = rec_in[s0 + i].x;
-            kbuf0[i] = ((k >> 24) << cbits) | (k & 0xFFFFFFu);
-            ibuf0[i] = (unsigned short)i;
+        const int passes = (kBkShift + cbits + 7) >> 3;  // 1..3
+        // keys and the digit counts of every pass
+        // every lane's key words are in flight at once (4-byte cp.async of
+        // each record's key field), so the bucket waits for one memory latency
+        for (int p = lane; p < E; p += 32)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(a + p)),
+                         "l"(&rec_in[s0 + p].x)
+                         : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        for (int i = lane; i < 3 * 128; i += 32) hist[i] = 0u;
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncwarp();
+        for (int p = lane; p < E; p += 32) {
+            const unsigned key = bk_key24(a[p], cbits);
+            a[p] = key;
+            for (int k = 0; k < passes; ++k) {
+                const unsigned d = (key >> (8 * k)) & 0xFFu;
+                atomicAdd(&hist[k * 128 + (d & 127u)], (d & 128u) ? 0x10000u : 1u);
+            }
         }
-        // positions split evenly over the warps (whole 32-element rounds); warp
-        // order is position order, so ranks stay stable
-        const int chunk = (((E + kBkSmallWarps - 1) / kBkSmallWarps) + 31) & ~31;
-        const int rounds = chunk / 32;
-        unsigned* kin = kbuf0;
-        unsigned* kout = kbuf1;
-        unsigned short* iin = ibuf0;
-        unsigned short* iout = ibuf1;
-        __syncthreads();
-        for (int pass = 0; pass < passes; ++pass) {
-            const int shift = 8 * pass;
-            for (int i = threadIdx.x; i < kBkSmallWarps * 256; i += kBkSmallThreads) wcount[i] = 0u;
-            __syncthreads();
-            unsigned rk[kBkRounds];
-            unsigned dg[kBkRounds];
+        __syncwarp();
+        unsigned* src = a;
+        unsigned* dst = b;
+        for (int k = 0; k < passes; ++k) {
+            // exclusive scan of the 256 digit counts; lane l owns digits 8l .. 8l+7
+            unsigned c[8], sum = 0;
 #pragma unroll
-            for (int r = 0; r < kBkRounds; ++r) {
-                if (r >= rounds) break;  // warp-uniform
-                const int pos = warp * chunk + r * 32 + lane;
-                const bool ok = pos < E && pos < (warp + 1) * chunk;
-                const unsigned d = ok ? ((kin[pos] >> shift) & 0xFFu) : 0x100u;
-                dg[r] = d;
+            for (int j = 0; j < 8; ++j) {
+                const int d = 8 * lane + j;
+                c[j] = (hist[k * 128 + (d & 127)] >> ((d & 128) ? 16 : 0)) & 0xFFFFu;
+                sum += c[j];
+            }
+            unsigned incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            unsigned run = incl - sum;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                base[8 * lane + j] = run;
+                run += c[j];
+            }
+            __syncwarp();
+            const int shift = k == 0 ? 0 : 8 * k + 3;
+            for (int p0 = 0; p0 < E; p0 += 32) {
+                const int p = p0 + lane;
+                const bool ok = p < E;
+                const unsigned v = ok ? src[p] : 0u;
+                const unsigned d = ok ? ((v >> shift) & 0xFFu) : 0x100u;
                 const unsigned peers = __match_any_sync(0xffffffffu, d);
-                unsigned prior = 0;
-                if (ok) prior = wcount[warp * 256 + d];
+                unsigned at = 0;
+                if (ok) at = base[d];
                 __syncwarp();
-                rk[r] = prior + __popc(peers & lt);
-                if (ok && (peers & lt) == 0u) wcount[warp * 256 + d] = prior + __popc(peers);
+                if (ok) {
+                    const unsigned before = peers & lt;
+                    dst[at + __popc(before)] = k == 0 ? (((v >> 8) << kBkWarpIdxBits) | (unsigned)p) : v;
+                    if (before == 0u) base[d] = at + __popc(peers);
+                }
                 __syncwarp();
             }
-            __syncthreads();
-            // digit totals, their exclusive scan, then per-(warp, digit) bases
-            const int dgt = threadIdx.x;  // 256 threads <-> 256 digits
-            unsigned tot = 0;
+            unsigned* t = src;
+            src = dst;
+            dst = t;
+        }
+        // src: entry indices in (row, col) order; dst: free for the keys
+        unsigned* const ord = src;
+        unsigned* const key = dst;
+        const unsigned cmask = (1u << cbits) - 1u;
+        constexpr int kG = 4;  // records in flight per lane
+        for (int p0 = lane; p0 < E; p0 += 32 * kG) {
+            uint4 r[kG];
 #pragma unroll
-            for (int ww = 0; ww < kBkSmallWarps; ++ww) tot += wcount[ww * 256 + dgt];
-            unsigned incl = tot;
+            for (int u = 0; u < kG; ++u)
+                if (p0 + 32 * u < E) r[u] = rec_in[s0 + (ord[p0 + 32 * u] & (kBkWarpCap - 1))];
 #pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const unsigned y = __shfl_up_sync(0xffffffffu, incl, d);
-                if (lane >= d) incl += y;
-            }
-            if (lane == 31) dbase[warp] = incl;
-            __syncthreads();
-            unsigned wpre = 0;
-            for (int ww = 0; ww < warp; ++ww) wpre += dbase[ww];
-            __syncthreads();
-            unsigned run = wpre + incl - tot;  // exclusive base of digit dgt
-            dbase[dgt] = run;
-#pragma unroll
-            for (int ww = 0; ww < kBkSmallWarps; ++ww) {
-                const unsigned c = wcount[ww * 256 + dgt];
-                wcount[ww * 256 + dgt] = run;
-                run += c;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int r = 0; r < kBkRounds; ++r) {
-                if (r >= rounds) break;
-                const int pos = warp * chunk + r * 32 + lane;
-                if (pos < E && pos < (warp + 1) * chunk) {
-                    const unsigned dst = wcount[warp * 256 + dg[r]] + rk[r];
-                    kout[dst] = kin[pos];
-                    iout[dst] = iin[pos];
+            for (int u = 0; u < kG; ++u) {
+                const int p = p0 + 32 * u;
+                if (p < E) {
+                    const unsigned k24 = bk_key24(r[u].x, cbits);
+                    key[p] = k24;
+                    I.csr_cols[e0 + p] = (int)(k24 & cmask);
+                    I.csr_vals[e0 + p] = bk_rec_val(r[u]);
                 }
             }
-            __syncthreads();
-            unsigned* tk = kin; kin = kout; kout = tk;
-            unsigned short* ti = iin; iin = iout; iout = ti;
         }
-        // kin/iin: sorted by (row, col); row starts from the row changes
-        const unsigned cmask = (1u << cbits) - 1u;
-        for (int p = threadIdx.x; p <= E; p += kBkSmallThreads) {
-            const int rp = p == 0 ? -1 : (int)(kin[p - 1] >> cbits);
-            const int rc = p == E ? kBkRows : (int)(kin[p] >> cbits);
-            for (int r = rp + 1; r <= rc && r < kBkRows; ++r) dbase[r] = (unsigned)p;
+        __syncwarp();
+        unsigned* const rowb = base;  // [kBkRows + 1]
+        for (int p = lane; p <= E; p += 32) {
+            const int rp = p == 0 ? -1 : (int)(key[p - 1] >> cbits);
+            const int rc = p == E ? kBkRows : (int)(key[p] >> cbits);
+            for (int r = rp + 1; r <= rc && r < kBkRows; ++r) rowb[r] = (unsigned)p;
         }
-        bk_order_equal_keys(kin, iin, E, rec_in + s0);
-        __syncthreads();
-        for (int p = threadIdx.x; p < E; p += kBkSmallThreads) {
-            I.csr_cols[e0 + p] = (int)(kin[p] & cmask);
-            I.csr_vals[e0 + p] = bk_rec_val(rec_in[s0 + iin[p]]);
+        if (lane == 0) rowb[kBkRows] = (unsigned)E;
+        // equal (row, col) keys in COO-position order (duplicates are rare)
+        for (int p = lane; p + 1 < E; p += 32) {
+            if (key[p + 1] != key[p] || (p > 0 && key[p - 1] == key[p])) continue;
+            int q = p + 2;
+            while (q < E && key[q] == key[p]) ++q;
+            for (int i = p + 1; i < q; ++i) {
+                const unsigned v = ord[i];
+                const unsigned kv = rec_in[s0 + (v & (kBkWarpCap - 1))].y;  // COO position
+                int j = i - 1;
+                while (j >= p && rec_in[s0 + (ord[j] & (kBkWarpCap - 1))].y > kv) {
+                    ord[j + 1] = ord[j];
+                    --j;
+                }
+                ord[j + 1] = v;
+            }
+            for (int i = p; i < q; ++i) I.csr_vals[e0 + i] = bk_rec_val(rec_in[s0 + (ord[i] & (kBkWarpCap - 1))]);
         }
-        for (int r = threadIdx.x; r <= nr; r += kBkSmallThreads) {
-            if (r < nr) I.row_ptr[r0 + r] = e0 + dbase[r];
+        __syncwarp();
+        for (int r = lane; r <= nr; r += 32) {
+            if (r < nr) I.row_ptr[r0 + r] = e0 + rowb[r];
             else if (r0 + nr == I.nrows) I.row_ptr[I.nrows] = I.nnz;
         }
-        // SpMV.  Rows of at most 32 entries: one lane per row, summed in column
-        // order (warps 0-1 cover the bucket's 64 rows).  Longer rows: a warp,
-        // lane i summing positions i, i+32, ..., then a fixed xor tree.  (On
-        // GB300 every FP64 warp instruction holds the FP64 pipe for ~64 cycles,
-        // so a tree per short row would cost more than the row itself.)
-        auto row_end = [&](int r) { return r + 1 < nr ? (int)dbase[r + 1] : E; };
-        if (warp < kBkRows / 32) {
-            const int r = warp * 32 + lane;
-            if (r < nr) {
-                const int a = (int)dbase[r], bb = row_end(r);
-                if (bb - a <= 32) {
-                    double acc = 0.0;
-                    for (int p = a; p < bb; ++p) {
-                        const unsigned c = kin[p] & cmask;
-                        acc = fma(bk_rec_val(rec_in[s0 + iin[p]]), c < I.ncols ? I.x[c] : 0.0, acc);
-                    }
-                    I.y[r0 + r] = acc;
-                }
-            }
-        }
-        for (int r = warp; r < nr; r += kBkSmallWarps) {
-            const int a = (int)dbase[r], bb = row_end(r);
-            if (bb - a <= 32) continue;  // warp-uniform
-            if (bb - a > 256) bad = true;  // a row above 256 entries: outside the contract
-            double acc = 0.0;
-            for (int p = a + lane; p < bb; p += 32) {
-                const unsigned c = kin[p] & cmask;
-                acc = fma(bk_rec_val(rec_in[s0 + iin[p]]), c < I.ncols ? I.x[c] : 0.0, acc);
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) I.y[r0 + r] = acc;
-        }
-        __syncthreads();
+        __syncwarp();
     }
-    if (bad) raise_error(err, ERRBIT_BOUNDS);
 }
 
 // Large buckets (up to 64 rows x 256): one CTA sorts the bucket's keys with a
@@ -468,7 +486,6 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
     unsigned* key = reinterpret_cast<unsigned*>(bk_smem);
     unsigned short* idx = reinterpret_cast<unsigned short*>(bk_smem + (size_t)kBkCap * 4);
     __shared__ int rstart[kBkRows + 1];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned nitems = *nitems_dev;
     unsigned it;
     bool bad = false;
@@ -525,30 +542,118 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
             if (r < nr) I.row_ptr[r0 + r] = e0 + rstart[r];
             else if (r0 + nr == I.nrows) I.row_ptr[I.nrows] = I.nnz;
         }
-        // SpMV as in the fast kernel: short rows one lane each, long rows a warp
-        if (warp < kBkRows / 32) {
-            const int r = warp * 32 + lane;
-            if (r < nr && rstart[r + 1] - rstart[r] <= 32) {
-                double acc = 0.0;
-                for (int p = rstart[r]; p < rstart[r + 1]; ++p) {
-                    const unsigned c = key[p] & 0xFFFFFFu;
-                    acc = fma(bk_rec_val(rec_in[s0 + idx[p]]), c < I.ncols ? I.x[c] : 0.0, acc);
-                }
-                I.y[r0 + r] = acc;
-            }
-        }
-        for (int r = warp; r < nr; r += kBkThreads / 32) {
-            if (rstart[r + 1] - rstart[r] <= 32) continue;  // warp-uniform
-            double acc = 0.0;
-            for (int p = rstart[r] + lane; p < rstart[r + 1]; p += 32) {
-                const unsigned c = key[p] & 0xFFFFFFu;
-                acc = fma(bk_rec_val(rec_in[s0 + idx[p]]), c < I.ncols ? I.x[c] : 0.0, acc);
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) I.y[r0 + r] = acc;
-        }
         __syncthreads();
+    }
+    if (bad) raise_error(err, ERRBIT_BOUNDS);
+}
+
+// ---- stage 5 ------------------------------------------------------------------
+// y[r] = the row's entries summed in column order as one fma chain (the
+// reference's sequential row loop, with fused multiply-adds), computed from
+// the finished CSR.  Each FP64 warp instruction holds the FP64 pipe for the
+// whole warp whatever its active lanes, so one lane per row only pays when
+// the 32 rows of a warp instruction have similar lengths: a warp takes a
+// 256-row chunk of one instance, counting-sorts its rows by length (256 bins,
+// lengths above 255 share the last) in shared memory, and gives each lane one
+// row of every group of 32 consecutive rows in that order.  Loads run kSpAhead
+// entries ahead of the (in-order) chain.  Rows above 256 entries are outside
+// the contract and reported.
+constexpr int kSpWarps = 8;
+constexpr int kSpPerSm = 4;
+constexpr int kSpAhead = 4;
+struct BkSpSmem {
+    unsigned cnt[256];
+    unsigned start[kSpRows];
+    unsigned short len[kSpRows];
+    unsigned char order[kSpRows];
+};
+
+__global__ void __launch_bounds__(kSpWarps * 32, kSpPerSm)
+    bk_spmv_kernel(const BkInst* __restrict__ inst, const BkItem* __restrict__ chunks, unsigned nchunks,
+                   unsigned* cursor, unsigned* err) {
+    __shared__ BkSpSmem sm_all[kSpWarps];
+    const int lane = threadIdx.x & 31;
+    BkSpSmem& sm = sm_all[threadIdx.x >> 5];
+    bool bad = false;
+    for (;;) {
+        unsigned it = 0;
+        if (lane == 0) it = atomicAdd(cursor, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= nchunks) break;
+        const BkItem w = chunks[it];
+        const BkInst I = inst[w.inst];
+        const long long r0 = (long long)w.tile * kSpRows;
+        const int nr = (int)((I.nrows - r0) < kSpRows ? (I.nrows - r0) : kSpRows);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) sm.cnt[lane + 32 * j] = 0u;
+        __syncwarp();
+        // row extents, kept inside [0, nnz] whatever the row pointers hold
+        for (int i = lane; i < nr; i += 32) {
+            long long a = I.row_ptr[r0 + i], e = I.row_ptr[r0 + i + 1];
+            a = a < 0 ? 0 : (a > I.nnz ? I.nnz : a);
+            e = e < a ? a : (e > I.nnz ? I.nnz : e);
+            const long long L = e - a;
+            bad |= L > 256;
+            const unsigned l = L > 0xFFFF ? 0xFFFFu : (unsigned)L;
+            sm.start[i] = (unsigned)a;
+            sm.len[i] = (unsigned short)l;
+            atomicAdd(&sm.cnt[l > 255u ? 255u : l], 1u);
+        }
+        __syncwarp();
+        {  // exclusive scan of the 256 bin counts; lane l owns bins 8l .. 8l+7
+            unsigned c[8], sum = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                c[j] = sm.cnt[8 * lane + j];
+                sum += c[j];
+            }
+            unsigned incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            unsigned run = incl - sum;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                sm.cnt[8 * lane + j] = run;
+                run += c[j];
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < nr; i += 32) {
+            const unsigned l = sm.len[i];
+            sm.order[atomicAdd(&sm.cnt[l > 255u ? 255u : l], 1u)] = (unsigned char)i;
+        }
+        __syncwarp();
+        const int* __restrict__ cols = I.csr_cols;
+        const double* __restrict__ vals = I.csr_vals;
+        const double* __restrict__ x = I.x;
+        const unsigned long long ncols = (unsigned long long)I.ncols;
+        for (int g = lane; g < nr; g += 32) {
+            const int i = sm.order[g];
+            const long long a = sm.start[i];
+            const int L = sm.len[i];
+            double acc = 0.0;
+            for (int k0 = 0; k0 < L; k0 += kSpAhead) {
+                double v[kSpAhead], xv[kSpAhead];
+#pragma unroll
+                for (int u = 0; u < kSpAhead; ++u) {
+                    v[u] = 0.0;
+                    xv[u] = 0.0;
+                    if (k0 + u < L) {
+                        const unsigned c = (unsigned)cols[a + k0 + u];
+                        v[u] = vals[a + k0 + u];
+                        if (c < ncols) xv[u] = x[c];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kSpAhead; ++u)
+                    if (k0 + u < L) acc = fma(v[u], xv[u], acc);
+            }
+            I.y[r0 + i] = acc;
+        }
+        __syncwarp();
     }
     if (bad) raise_error(err, ERRBIT_BOUNDS);
 }
@@ -560,7 +665,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     Device* d = nullptr;
     HYD_TRY(device(&d));
     std::vector<BkInst> inst(bi.size());
-    long long nb_total = 0, entries = 0, nt_total = 0;
+    long long nb_total = 0, entries = 0, nt_total = 0, nc_total = 0;
     for (size_t i = 0; i < bi.size(); ++i) {
         const BatchInst& B = bi[i];
         if (B.ncols >= (1LL << 24) || B.nrows >= (1LL << 31)) return HYD_CUDA_ERR_UNSUPPORTED;
@@ -580,19 +685,21 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
         I.csr_vals = B.csr_vals;
         I.y = B.y;
         I.tile_base = nt_total;
+        I.chunk_base = nc_total;
         nt_total += (B.nnz + kTileEntries - 1) / kTileEntries;
+        nc_total += (B.nrows + kSpRows - 1) / kSpRows;
         nb_total += I.nbuckets;
         entries += B.nnz;
     }
-    if (nb_total >= (1LL << 31) || nt_total >= (1LL << 31) || entries >= (1LL << 32))
+    if (nb_total >= (1LL << 31) || nt_total >= (1LL << 31) || nc_total >= (1LL << 31) || entries >= (1LL << 32))
         return HYD_CUDA_ERR_UNSUPPORTED;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t inst_b = al(inst.size() * sizeof(BkInst)), tiles_b = al((size_t)nt_total * sizeof(BkItem)),
-                 bk_b = al((size_t)nb_total * sizeof(BkItem));
+                 bk_b = al((size_t)nb_total * sizeof(BkItem)), ch_b = al((size_t)nc_total * sizeof(BkItem));
     const size_t cnt_b = al((size_t)nb_total * 4), wide_b = al((size_t)nb_total * 8);
     const size_t vals_b = al((size_t)entries * 8);
     void* buf = nullptr;
-    HYD_TRY(device_buffer(d, key, inst_b + tiles_b + 2 * bk_b + 2 * cnt_b + 2 * wide_b + vals_b + vals_b + 256,
+    HYD_TRY(device_buffer(d, key, inst_b + tiles_b + 2 * bk_b + ch_b + 2 * cnt_b + 2 * wide_b + vals_b + vals_b + 256,
                           &buf));
     unsigned char* b = static_cast<unsigned char*>(buf);
     size_t off = 0;
@@ -610,6 +717,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     long long* bstart = reinterpret_cast<long long*>(take(wide_b));
     uint4* recs = reinterpret_cast<uint4*>(take(2 * vals_b));  // (key, COO position, value) per entry
     BkItem* overflow = reinterpret_cast<BkItem*>(take(bk_b));
+    BkItem* d_chunks = reinterpret_cast<BkItem*>(take(ch_b));
     unsigned* cursors = reinterpret_cast<unsigned*>(take(256));
     // only the instance table crosses from the host; the work lists are
     // written by bk_items_kernel
@@ -623,7 +731,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     {
         const int64_t ni = (int64_t)inst.size();
         const unsigned g = (unsigned)(ni < 4096 ? ni : 4096);
-        bk_items_kernel<<<g, 256, 0, s>>>(d_inst, ni, d_tiles, d_bk);
+        bk_items_kernel<<<g, 256, 0, s>>>(d_inst, ni, d_tiles, d_bk, d_chunks);
         HYD_TRY(launch_check("bk_items"));
     }
     const size_t n_tiles = (size_t)nt_total, n_buckets = (size_t)nb_total;
@@ -644,14 +752,20 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
                                                              bfill, recs, d->d_err);
         HYD_TRY(launch_check("bk_split"));
     }
-    HYD_TRY(configure_kernel((const void*)bk_bucket_small_kernel, d, false));
-    bk_bucket_small_kernel<<<(unsigned)(d->sm_count * kBkSmallPerSm), kBkSmallThreads, kBkSmallSmem, s>>>(
+    HYD_TRY(configure_kernel((const void*)bk_bucket_warp_kernel, d, false));
+    bk_bucket_warp_kernel<<<(unsigned)(d->sm_count * kBkWarpPerSm), kBkWarpWarps * 32, kBkWarpSmem, s>>>(
         d_inst, d_bk, (unsigned)n_buckets, cursors + 2, bstart, bcount, recs, overflow, cursors + 4, d->d_err);
-    HYD_TRY(launch_check("bk_bucket_small"));
+    HYD_TRY(launch_check("bk_bucket_warp"));
     HYD_TRY(configure_kernel((const void*)bk_bucket_kernel, d, false));
     bk_bucket_kernel<<<grid, kBkThreads, kBkSmem, s>>>(d_inst, overflow, cursors + 4, cursors + 3, bstart, bcount,
                                                        recs, d->d_err);
     HYD_TRY(launch_check("bk_bucket_large"));
+    if (nc_total) {
+        bk_spmv_kernel<<<(unsigned)(d->sm_count * kSpPerSm), kSpWarps * 32, 0, s>>>(d_inst, d_chunks,
+                                                                                  (unsigned)nc_total, cursors + 5,
+                                                                                  d->d_err);
+        HYD_TRY(launch_check("bk_spmv"));
+    }
     if (!async_tables) HYD_CUDA_TRY(cudaStreamSynchronize(s));
     return HYD_CUDA_OK;
 }

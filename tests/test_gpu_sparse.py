@@ -205,6 +205,28 @@ def test_batched_pipeline_duplicates_keep_coo_order(hc, orc, dev, pipeline, monk
     _check_batch(hc, orc, desc, rows, cols, vals, x, *out)
 
 
+def test_batched_pipeline_column_widths(hc, orc, dev):
+    """Column counts that give the bucket sort one, two and three 8-bit passes
+    (ncols 1 .. 2^18), and wider instances (ncols 2^18 + 1, 2^20) whose
+    buckets go to the block-wide kernel, in one batch."""
+    rng = np.random.default_rng(59)
+    descs, R, Cc, V, X = [], [], [], [], []
+    for n, ncols, nnz in ((70, 1, 60), (130, 4, 700), (90, 5, 900), (200, 256, 4000), (150, 257, 3000),
+                          (3000, 1 << 18, 40000), (2000, (1 << 18) + 1, 30000), (1000, 1 << 20, 20000)):
+        r = rng.integers(0, n, nnz)
+        c = rng.integers(0, ncols, nnz)
+        descs.append((n, ncols, nnz))
+        R.append(r); Cc.append(c); V.append(rng.uniform(-1, 1, nnz)); X.append(rng.uniform(-1, 1, ncols))
+    desc = np.array(descs, dtype=np.int64)
+    rows = torch.from_numpy(np.concatenate(R).astype(np.int32)).to(dev)
+    cols = torch.from_numpy(np.concatenate(Cc).astype(np.int32)).to(dev)
+    vals = torch.from_numpy(np.concatenate(V)).to(dev)
+    x = torch.from_numpy(np.concatenate(X)).to(dev)
+    out = hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
+    hc.check(hc.device_check())
+    _check_batch(hc, orc, desc, rows, cols, vals, x, *out)
+
+
 @pytest.mark.parametrize("pipeline", ["bucketed", "rows"])
 @pytest.mark.parametrize("bad", ["row", "col"])
 def test_batched_out_of_range_entry_reported(hc, orc, dev, pipeline, bad, monkeypatch):
