@@ -208,28 +208,63 @@ __device__ __forceinline__ void bulk_load_1d(unsigned dst, const void* src, unsi
         : "memory");
 }
 
-// ---- decoupled look-back: bounded wait on a window of tile status flags -------
+// ---- decoupled look-back: tile status words and the bounded window wait ------
 constexpr unsigned kSpinLimit = 1u << 22;  // polls before a look-back gives up
 
 __device__ __forceinline__ unsigned ld_volatile_u32(const unsigned* p) { return *(volatile const unsigned*)p; }
 
-// Warp-wide: lane l watches the status flag of tile q = p - l (q < 0: before
-// the first tile, reported as 2 = "inclusive prefix known").  Polls until every
-// lane's flag is non-zero and returns this lane's flag, or returns 0 on every
-// lane when `limit` polls went by without that (the caller raises
-// ERRBIT_TIMEOUT and abandons the look-back).  Flags are published with a
-// __threadfence() before the volatile store, so the caller fences once after a
-// successful return before reading the published values.
-__device__ __forceinline__ unsigned lookback_wait_window(const unsigned* flags, int64_t p, int lane,
-                                                         unsigned limit = kSpinLimit) {
+// One tile's status: flag 0 = nothing published, 1 = `bits` hold the tile's
+// aggregate, 2 = `bits` hold the inclusive prefix through the tile.  A status
+// is written and read as one 16-byte access, so a reader gets a flag together
+// with its own value in a single memory round trip and a publisher needs no
+// fence between value and flag (the value and flag cannot be seen apart).
+struct __align__(16) TileWord {
+    unsigned long long flag;
+    unsigned long long bits;
+};
+
+__device__ __forceinline__ void tile_word_store(TileWord* w, unsigned long long flag, unsigned long long bits) {
+    asm volatile("st.volatile.global.v2.u64 [%0], {%1, %2};" ::"l"(w), "l"(flag), "l"(bits) : "memory");
+}
+__device__ __forceinline__ void tile_word_load(const TileWord* w, unsigned long long& flag,
+                                               unsigned long long& bits) {
+    asm volatile("ld.volatile.global.v2.u64 {%0, %1}, [%2];" : "=l"(flag), "=l"(bits) : "l"(w) : "memory");
+}
+
+template <class T>
+__device__ __forceinline__ unsigned long long to_bits(T v) {
+    return (unsigned long long)v;
+}
+template <>
+__device__ __forceinline__ unsigned long long to_bits<double>(double v) {
+    return (unsigned long long)__double_as_longlong(v);
+}
+template <class T>
+__device__ __forceinline__ T from_bits(unsigned long long b) {
+    return (T)b;
+}
+template <>
+__device__ __forceinline__ double from_bits<double>(unsigned long long b) {
+    return __longlong_as_double((long long)b);
+}
+
+// Warp-wide: lane l watches the status word of tile q = p - l (q < 0: before
+// the first tile, reported as flag 2 with bits 0).  Polls until every lane's
+// flag is non-zero and returns this lane's flag with its value in `bits`, or
+// returns 0 on every lane when `limit` polls went by without that (the caller
+// raises ERRBIT_TIMEOUT and abandons the look-back).
+__device__ __forceinline__ unsigned lookback_wait_words(const TileWord* words, int64_t p, int lane,
+                                                        unsigned long long& bits, unsigned limit = kSpinLimit) {
     const int64_t q = p - lane;
-    unsigned f = q >= 0 ? ld_volatile_u32(&flags[q]) : 2u;
+    unsigned long long f = 2ull;
+    bits = 0ull;
+    if (q >= 0) tile_word_load(&words[q], f, bits);
     unsigned spins = 0;
-    while (__any_sync(0xffffffffu, f == 0u)) {
+    while (__any_sync(0xffffffffu, f == 0ull)) {
         if (++spins > limit) return 0u;
-        if (f == 0u) f = ld_volatile_u32(&flags[q]);
+        if (f == 0ull) tile_word_load(&words[q], f, bits);
     }
-    return f;
+    return (unsigned)f;
 }
 
 }  // namespace hyd

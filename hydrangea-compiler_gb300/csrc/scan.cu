@@ -47,6 +47,12 @@ constexpr int kScanT = 512;
 constexpr int kScanIPT = 8;
 constexpr int kScanTile = kScanT * kScanIPT;  // 4096 (32 KiB of static shared memory for int64)
 constexpr int kScanCtasPerSm = 4;  // resident CTAs per SM (32 registers per thread)
+// Tiles sit in shared memory with one 8-byte pad after every 16 elements: a
+// thread's blocked run of 8 (stride 64 B between lanes) and the striped
+// accesses then both meet no bank conflict.  Unpadded, the blocked accesses
+// were 16-way conflicted and the tile copy alone ran at half the copy rate.
+constexpr int kScanTileP = kScanTile + kScanTile / 16;
+__device__ __forceinline__ int scan_pad(int i) { return i + (i >> 4); }
 
 // --- block-wide exclusive scan of one value per thread (int64, wrapping) ------
 template <class T>
@@ -91,10 +97,10 @@ __device__ __forceinline__ void tile_load(const T* in, int64_t n, int64_t base, 
         v[j] = k < n ? in[reverse ? (n - 1 - k) : k] : T(0);
     }
 #pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) sh[threadIdx.x + j * kScanT] = v[j];
+    for (int j = 0; j < kScanIPT; ++j) sh[scan_pad(threadIdx.x + j * kScanT)] = v[j];
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) items[j] = sh[threadIdx.x * kScanIPT + j];
+    for (int j = 0; j < kScanIPT; ++j) items[j] = sh[scan_pad(threadIdx.x * kScanIPT + j)];
     __syncthreads();
 }
 
@@ -102,31 +108,27 @@ template <class T>
 __device__ __forceinline__ void tile_store(T* out, int64_t n, int64_t base, bool reverse, T* sh,
                                            const T (&items)[kScanIPT]) {
 #pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) sh[threadIdx.x * kScanIPT + j] = items[j];
+    for (int j = 0; j < kScanIPT; ++j) sh[scan_pad(threadIdx.x * kScanIPT + j)] = items[j];
     __syncthreads();
     for (int i = threadIdx.x; i < kScanTile; i += kScanT) {
         const int64_t k = base + i;
-        if (k < n) out[reverse ? (n - 1 - k) : k] = sh[i];
+        if (k < n) out[reverse ? (n - 1 - k) : k] = sh[scan_pad(i)];
     }
 }
 
 // ---- int64 decoupled look-back ----------------------------------------------------
-// Status per tile: flag (0 none, 1 aggregate, 2 inclusive prefix) + two values.
+// One TileWord per tile (flag 0 none, 1 aggregate, 2 inclusive prefix).
 struct ScanStatus {
-    unsigned* flag;
-    long long* aggregate;
-    long long* inclusive;
+    TileWord* word;
     unsigned* tile_counter;
 };
-
-__device__ __forceinline__ long long ld_volatile_i64(const long long* p) { return *(volatile const long long*)p; }
 
 __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_i64_lookback_kernel(const long long* __restrict__ in,
                                                                     long long* __restrict__ out, int64_t n,
                                                                     long long init, bool reverse,
                                                                     bool inclusive, ScanStatus st,
                                                                     unsigned* err) {
-    __shared__ long long sh_tile[kScanTile];
+    __shared__ long long sh_tile[kScanTileP];
     __shared__ long long sh_scan[33];
     __shared__ unsigned sh_tile_id;
     __shared__ long long sh_prefix;
@@ -148,46 +150,37 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_i64_lookback_kern
         const int lane = threadIdx.x;
         if (tile == 0) {
             if (lane == 0) {
-                st.inclusive[0] = init + agg;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[0] = 2u;
+                tile_word_store(&st.word[0], 2ull, to_bits(init + agg));
                 sh_prefix = init;
             }
         } else {
-            if (lane == 0) {
-                st.aggregate[tile] = agg;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[tile] = 1u;
-            }
+            if (lane == 0) tile_word_store(&st.word[tile], 1ull, to_bits(agg));
             long long running = 0;
             int64_t p = (int64_t)tile - 1;  // window covers p, p-1, ..., p-31
-            bool done = false;
-            while (!done) {
+            for (;;) {
                 const int64_t q = p - lane;
                 // wait until every tile of the window has published something
-                const unsigned f = lookback_wait_window(st.flag, p, lane);
+                unsigned long long bits;
+                const unsigned f = lookback_wait_words(st.word, p, lane, bits);
                 if (f == 0u) {
                     if (lane == 0) raise_error(err, ERRBIT_TIMEOUT);
                     break;
                 }
-                __threadfence();
                 const unsigned incl_mask = __ballot_sync(0xffffffffu, f == 2u);
-                // nearest predecessor with an inclusive prefix (lowest lane)
+                // nearest predecessor with an inclusive prefix (lowest lane):
+                // the aggregates of the lanes before it, then its prefix (before
+                // tile 0: the fold's initial value)
                 const int stop = incl_mask ? (__ffs(incl_mask) - 1) : 32;
                 long long v = 0;
-                if (lane < stop && q >= 0) v = ld_volatile_i64(&st.aggregate[q]);
-                if (lane == stop && q >= 0) v = ld_volatile_i64(&st.inclusive[q]);
-                if (lane == stop && q < 0) v = init;  // before tile 0: the fold's initial value
+                if (lane <= stop) v = q >= 0 ? from_bits<long long>(bits) : init;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
                 running += v;
-                if (stop < 32) done = true;
+                if (stop < 32) break;
                 p -= 32;
             }
             if (lane == 0) {
-                st.inclusive[tile] = running + agg;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[tile] = 2u;
+                tile_word_store(&st.word[tile], 2ull, to_bits(running + agg));
                 sh_prefix = running;
             }
         }
@@ -209,22 +202,16 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_i64_lookback_kern
 }
 
 // ---- deterministic decoupled look-back (left fold) -----------------------------------
-// Status per tile: flag (0 none, 1 aggregate, 2 inclusive) and the two values.
+// One TileWord per tile (flag 0 none, 1 aggregate, 2 inclusive prefix; T's
+// bits as the value).
 template <class T>
 struct FoldStatus {
-    unsigned* flag;
-    T* aggregate;
-    T* inclusive;
+    TileWord* word;
     unsigned* tile_counter;
     unsigned* bad;  // segmented reduce: the offsets are not a valid partition
 };
 constexpr int kFoldBuf = 1024;                // aggregates one look-back may collect before it restarts
 constexpr unsigned kFoldRestarts = 1u << 12;  // restarts before a look-back gives up
-
-template <class T>
-__device__ __forceinline__ T ld_volatile(const T* p) {
-    return *(volatile const T*)p;
-}
 
 // Warp-wide (all 32 lanes of one warp).  The exclusive prefix of `tile`, as
 // the left fold inclusive[s] + aggregate[s+1] + ... + aggregate[tile-1] where s
@@ -249,16 +236,15 @@ __device__ bool lookback_fold(const FoldStatus<T>& st, int64_t tile, T before, T
     int cnt = 0;
     T base = before;
     for (;;) {
-        const unsigned f = lookback_wait_window(st.flag, p, lane);
+        unsigned long long bits;
+        const unsigned f = lookback_wait_words(st.word, p, lane, bits);
         if (f == 0u) return false;
-        __threadfence();
         const int64_t q = p - lane;
         const unsigned incl = __ballot_sync(0xffffffffu, f == 2u);
         const int stop = incl ? __ffs(incl) - 1 : 32;
-        if (lane < stop) sbuf[cnt + lane] = ld_volatile(&st.aggregate[q]);
+        if (lane < stop) sbuf[cnt + lane] = from_bits<T>(bits);  // aggregates, nearest first
         if (stop < 32) {
-            T b = before;
-            if (lane == stop && q >= 0) b = ld_volatile(&st.inclusive[q]);
+            const T b = q >= 0 ? from_bits<T>(bits) : before;
             base = __shfl_sync(0xffffffffu, b, stop);
             cnt += stop;
             break;
@@ -282,20 +268,30 @@ __device__ bool lookback_fold(const FoldStatus<T>& st, int64_t tile, T before, T
     prefix = __shfl_sync(0xffffffffu, acc, 0);
     if (kHelp) {
         __syncwarp();
-        for (int i = lane; i < cnt; i += 32) st.inclusive[tile - 1 - i] = sbuf[i];
-        __threadfence();
-        __syncwarp();
-        for (int i = lane; i < cnt; i += 32) *(volatile unsigned*)&st.flag[tile - 1 - i] = 2u;
+        for (int i = lane; i < cnt; i += 32) tile_word_store(&st.word[tile - 1 - i], 2ull, to_bits(sbuf[i]));
     }
     return true;
 }
 
-// float64 (and any T) scan with the left-fold look-back.
+// float64 (and any T) scan, deterministic in two levels.  Tiles form blocks
+// of 32 (block k = tiles 32k .. 32k+31):
+//  * within a block, tile i's prefix over its block-mates is the value at lane
+//    i-1 of a warp inclusive scan (fixed shuffle tree) of the block's tile
+//    aggregates, and the block total T(k) is its lane-31 value;
+//  * across blocks, B(k) = the left fold of T(0), ..., T(k) onto init, found
+//    through lookback_fold over per-block status words (the last tile of a
+//    block publishes T(k), then B(k));
+//  * the tile's exclusive prefix is B(k-1) + (its within-block prefix).
+// Every value is defined by the data alone, not by timing, so results are
+// run-to-run identical.  A single-level left fold over tile aggregates puts
+// one dependent FP64 add per tile on the scan's critical path (about 76
+// cycles each on this part: 1.3 ms at 2^27); here the dependent chain is one
+// add per block of 32 tiles.
 template <class T>
 __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_fold_kernel(const T* __restrict__ in, T* __restrict__ out, int64_t n,
                                                             T init, bool reverse, bool inclusive, FoldStatus<T> st,
-                                                            unsigned* err) {
-    __shared__ T sh_tile[kScanTile];
+                                                            FoldStatus<T> bst, unsigned* err) {
+    __shared__ T sh_tile[kScanTileP];
     __shared__ T sh_scan[33];
     __shared__ T sh_fold[kFoldBuf];
     __shared__ unsigned sh_tile_id;
@@ -313,29 +309,35 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_fold_kernel(const
     const T texcl = block_exclusive_scan(tsum, sh_scan, agg);
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
-        if (tile == 0) {
-            if (lane == 0) {
-                st.inclusive[0] = init + agg;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[0] = 2u;
-                sh_prefix = init;
+        const int64_t blk = tile >> 5;
+        const int pos = (int)(tile & 31u);
+        if (lane == 0) tile_word_store(&st.word[tile], 1ull, to_bits(agg));
+        // the aggregates of the block's tiles before this one (earlier tickets)
+        unsigned long long f = 1ull, bits = 0ull;
+        if (lane < pos) tile_word_load(&st.word[(blk << 5) + lane], f, bits);
+        unsigned spins = 0;
+        bool ok = true;
+        while (__any_sync(0xffffffffu, f == 0ull)) {
+            if (++spins > kSpinLimit) {
+                ok = false;
+                break;
             }
-        } else {
-            if (lane == 0) {
-                st.aggregate[tile] = agg;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[tile] = 1u;
-            }
-            T prefix = T(0);
-            if (!lookback_fold<false>(st, tile, init, sh_fold, prefix) && lane == 0)
-                raise_error(err, ERRBIT_TIMEOUT);
-            if (lane == 0) {
-                st.inclusive[tile] = prefix + agg;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[tile] = 2u;
-                sh_prefix = prefix;
-            }
+            if (f == 0ull) tile_word_load(&st.word[(blk << 5) + lane], f, bits);
         }
+        if (!ok && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
+        T sc = lane < pos ? from_bits<T>(bits) : (lane == pos ? agg : T(0));
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const T y = __shfl_up_sync(0xffffffffu, sc, d);
+            if (lane >= d) sc = y + sc;
+        }
+        const T within = __shfl_sync(0xffffffffu, sc, pos > 0 ? pos - 1 : 0);
+        const T total = __shfl_sync(0xffffffffu, sc, 31);
+        if (pos == 31 && lane == 0) tile_word_store(&bst.word[blk], 1ull, to_bits(total));
+        T before = init;  // B(blk - 1)
+        if (!lookback_fold<false>(bst, blk, init, sh_fold, before) && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
+        if (pos == 31 && lane == 0) tile_word_store(&bst.word[blk], 2ull, to_bits(before + total));
+        if (lane == 0) sh_prefix = pos == 0 ? before : before + within;
     }
     __syncthreads();
     T acc = sh_prefix + texcl;
@@ -386,7 +388,7 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
                                                                  const T* __restrict__ vals, int64_t n_vals, T init,
                                                                  T* __restrict__ out, FoldStatus<T> st,
                                                                  int64_t ntiles, unsigned* err) {
-    __shared__ T sh_run[kScanTile];  // the tile's values, then the running segment sums
+    __shared__ T sh_run[kScanTileP];  // the tile's values, then the running segment sums (padded)
     __shared__ unsigned sh_head[kScanTile / 32];
     __shared__ T sh_fold[kFoldBuf];
     __shared__ T sh_wv[32];
@@ -418,7 +420,7 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
             v[j] = i < cnt ? vals[v0 + i] : T(0);
         }
 #pragma unroll
-        for (int j = 0; j < kScanIPT; ++j) sh_run[threadIdx.x + j * kScanT] = v[j];
+        for (int j = 0; j < kScanIPT; ++j) sh_run[scan_pad(threadIdx.x + j * kScanT)] = v[j];
     }
     __syncthreads();
     const int64_t sb = sh_sb, se = sh_se;
@@ -437,9 +439,8 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
     if (__syncthreads_or(bad)) {
         if (threadIdx.x == 0) {
             atomicOr(st.bad, 1u);
-            st.inclusive[tile] = T(0);  // successors must not wait; the per-segment pass redoes every sum
-            __threadfence();
-            *(volatile unsigned*)&st.flag[tile] = 2u;
+            // successors must not wait; the per-segment pass redoes every sum
+            tile_word_store(&st.word[tile], 2ull, to_bits(T(0)));
         }
         return;
     }
@@ -448,7 +449,7 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
     const unsigned hb = (sh_head[p0 >> 5] >> (p0 & 31)) & 0xffu;
     T x[kScanIPT];
 #pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) x[j] = sh_run[p0 + j];
+    for (int j = 0; j < kScanIPT; ++j) x[j] = sh_run[scan_pad(p0 + j)];
     bool h = hb != 0u;
     T v = T(0);
 #pragma unroll
@@ -496,41 +497,27 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
 #pragma unroll
     for (int j = 0; j < kScanIPT; ++j) {
         r = (hb >> j) & 1u ? x[j] : r + x[j];
-        sh_run[p0 + j] = r;
+        sh_run[scan_pad(p0 + j)] = r;
     }
     const bool any_head = __syncthreads_or(h);
     // publish and look back (warp 0)
     if (warp == 0) {
-        const T tail = cnt > 0 ? sh_run[cnt - 1] : T(0);
-        if (lane == 0) {
-            if (any_head || !open) {
-                st.inclusive[tile] = tail;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[tile] = 2u;
-            } else {
-                st.aggregate[tile] = tail;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[tile] = 1u;
-            }
-        }
+        const T tail = cnt > 0 ? sh_run[scan_pad(cnt - 1)] : T(0);
+        if (lane == 0) tile_word_store(&st.word[tile], (any_head || !open) ? 2ull : 1ull, to_bits(tail));
         T carry = T(0);
         if (open) {
             if (!lookback_fold<true>(st, tile, T(0), sh_fold, carry) && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
-            if (lane == 0 && !any_head) {
-                st.inclusive[tile] = carry + tail;
-                __threadfence();
-                *(volatile unsigned*)&st.flag[tile] = 2u;
-            }
+            if (lane == 0 && !any_head) tile_word_store(&st.word[tile], 2ull, to_bits(carry + tail));
         }
         if (lane == 0) sh_carry = carry;
     }
     __syncthreads();
     if (open && end_open <= v0 + cnt && threadIdx.x == 0)
-        out[sb - 1] = init + (sh_carry + sh_run[end_open - 1 - v0]);
+        out[sb - 1] = init + (sh_carry + sh_run[scan_pad((int)(end_open - 1 - v0))]);
     for (int64_t s = sb + threadIdx.x; s < se; s += kScanT) {
         const int64_t o = offsets[s], e = offsets[s + 1];
         if (e == o) out[s] = init;
-        else if (e <= v0 + cnt) out[s] = init + sh_run[e - 1 - v0];
+        else if (e <= v0 + cnt) out[s] = init + sh_run[scan_pad((int)(e - 1 - v0))];
     }
 }
 
@@ -571,8 +558,7 @@ namespace hyd {
 // Scratch bytes the decoupled look-back needs for n elements.
 size_t scan_i64_scratch_bytes(int64_t n) {
     const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
-    const size_t flag_bytes = ((size_t)ntiles * 4 + 255) & ~(size_t)255;
-    return flag_bytes + 16 * (size_t)ntiles + 256;
+    return sizeof(TileWord) * (size_t)ntiles + 256;  // + room to align the words to 16 bytes
 }
 
 // int64 scan with caller-provided status scratch (scan_i64_scratch_bytes(n))
@@ -583,13 +569,10 @@ int scan_i64_launch_with(const long long* in, long long* out, int64_t n, long lo
     Device* d = nullptr;
     HYD_TRY(device(&d));
     const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
-    const size_t flag_bytes = ((size_t)ntiles * 4 + 255) & ~(size_t)255;
     ScanStatus st;
-    st.flag = static_cast<unsigned*>(status_scratch);
-    st.aggregate = reinterpret_cast<long long*>(static_cast<unsigned char*>(status_scratch) + flag_bytes);
-    st.inclusive = st.aggregate + ntiles;
+    st.word = reinterpret_cast<TileWord*>((reinterpret_cast<uintptr_t>(status_scratch) + 15) & ~(uintptr_t)15);
     st.tile_counter = tile_counter;
-    HYD_CUDA_TRY(cudaMemsetAsync(st.flag, 0, (size_t)ntiles * 4, stream));
+    HYD_CUDA_TRY(cudaMemsetAsync(st.word, 0, sizeof(TileWord) * (size_t)ntiles, stream));
     HYD_CUDA_TRY(cudaMemsetAsync(st.tile_counter, 0, 4, stream));
     scan_i64_lookback_kernel<<<(unsigned)ntiles, kScanT, 0, stream>>>(in, out, n, init, reverse, inclusive, st,
                                                                        d->d_err);
@@ -616,22 +599,26 @@ extern "C" int hyd_cuda_scan_i64(const int64_t* in, int64_t* out, int64_t n, int
                            reverse != 0, inclusive != 0, as_stream(stream));
 }
 
-// Status scratch of the left-fold look-back for `ntiles` tiles of 8-byte
-// values: [0, 256) the tile counter (+0) and the invalid-offsets word (+4),
-// then the flags, then the aggregates and inclusive values.  The first
-// 256 + 4 * ntiles bytes are zeroed on the stream (one memset).
+// Status scratch of the left-fold look-back for `ntiles` tiles of (at most)
+// 8-byte values: [0, 256) the tile counter (+0) and the invalid-offsets word
+// (+4), then `ntiles` tile words and, when `bst` is given, one word per block
+// of 32 tiles; all of it zeroed on the stream (one memset).
 template <class T>
-static int fold_status(cudaStream_t s, int64_t ntiles, FoldStatus<T>* st) {
-    const size_t flag_bytes = ((size_t)ntiles * 4 + 255) & ~(size_t)255;
+static int fold_status(cudaStream_t s, int64_t ntiles, FoldStatus<T>* st, FoldStatus<T>* bst = nullptr) {
+    static_assert(sizeof(T) <= 8, "a tile word holds a value of at most 8 bytes");
+    const int64_t nblocks = bst ? (ntiles + 31) / 32 : 0;
+    const size_t bytes = 256 + sizeof(TileWord) * (size_t)(ntiles + nblocks);
     void* scratch = nullptr;
-    HYD_TRY(workspace(s, 256 + flag_bytes + 2 * sizeof(T) * (size_t)ntiles, nullptr, &scratch));
-    unsigned char* b = static_cast<unsigned char*>(scratch);
+    HYD_TRY(workspace(s, bytes, nullptr, &scratch));
+    unsigned char* b = static_cast<unsigned char*>(scratch);  // 256-byte aligned
     st->tile_counter = reinterpret_cast<unsigned*>(b);
     st->bad = reinterpret_cast<unsigned*>(b + 4);
-    st->flag = reinterpret_cast<unsigned*>(b + 256);
-    st->aggregate = reinterpret_cast<T*>(b + 256 + flag_bytes);
-    st->inclusive = st->aggregate + ntiles;
-    HYD_CUDA_TRY(cudaMemsetAsync(b, 0, 256 + (size_t)ntiles * 4, s));
+    st->word = reinterpret_cast<TileWord*>(b + 256);
+    if (bst) {
+        *bst = *st;
+        bst->word = st->word + ntiles;
+    }
+    HYD_CUDA_TRY(cudaMemsetAsync(b, 0, bytes, s));
     return HYD_CUDA_OK;
 }
 
@@ -645,10 +632,10 @@ extern "C" int hyd_cuda_scan_f64(const double* in, double* out, int64_t n, doubl
     HYD_CHECK_ARG(ntiles <= 0x7fffffffLL, "scan_f64: too long");
     Device* d = nullptr;
     HYD_TRY(device(&d));
-    FoldStatus<double> st;
-    HYD_TRY(fold_status(s, ntiles, &st));
+    FoldStatus<double> st, bst;
+    HYD_TRY(fold_status(s, ntiles, &st, &bst));
     scan_fold_kernel<double><<<(unsigned)ntiles, kScanT, 0, s>>>(in, out, n, init, reverse != 0, inclusive != 0, st,
-                                                                 d->d_err);
+                                                                 bst, d->d_err);
     return launch_check("scan_f64");
 }
 

@@ -48,12 +48,13 @@ __global__ void selftest_mbar_timeout_kernel(unsigned limit, unsigned* err) {
     }
 }
 
-// Timeout self-test 1: one warp looks back over 32 tile status flags that are
+// Timeout self-test 1: one warp looks back over 32 tile status words that are
 // all zero ("nothing published"), through the wait the scans use.
-__global__ void selftest_lookback_timeout_kernel(const unsigned* flags, unsigned limit, unsigned* err) {
+__global__ void selftest_lookback_timeout_kernel(const TileWord* words, unsigned limit, unsigned* err) {
     const int lane = threadIdx.x & 31;
     if (threadIdx.x < 32) {
-        const unsigned f = lookback_wait_window(flags, 31, lane, limit);
+        unsigned long long bits;
+        const unsigned f = lookback_wait_words(words, 31, lane, bits, limit);
         if (f == 0u && lane == 0) raise_error(err, ERRBIT_TIMEOUT);
     }
 }
@@ -83,9 +84,9 @@ extern "C" int hyd_cuda_selftest_timeout(int which, uint32_t poll_limit, void* s
         selftest_mbar_timeout_kernel<<<1, 32, 0, s>>>(poll_limit, d->d_err);
     } else {
         void* scratch = nullptr;
-        HYD_TRY(workspace(s, 32 * sizeof(unsigned), nullptr, &scratch));
-        HYD_CUDA_TRY(cudaMemsetAsync(scratch, 0, 32 * sizeof(unsigned), s));
-        selftest_lookback_timeout_kernel<<<1, 32, 0, s>>>(static_cast<const unsigned*>(scratch), poll_limit,
+        HYD_TRY(workspace(s, 32 * sizeof(TileWord), nullptr, &scratch));
+        HYD_CUDA_TRY(cudaMemsetAsync(scratch, 0, 32 * sizeof(TileWord), s));
+        selftest_lookback_timeout_kernel<<<1, 32, 0, s>>>(static_cast<const TileWord*>(scratch), poll_limit,
                                                           d->d_err);
     }
     return launch_check("selftest_timeout");
