@@ -571,13 +571,17 @@ __global__ void __launch_bounds__(kPartThreads, kPartCtasPerSm)
         const bool full = have == kPartTile;
         unsigned hi_or = 0u;  // high words: all zero -> staged as 4-byte records
         bool fast = false;
+        // thread t holds elements 2(t + q kPartThreads) + {0, 1}, q < 4: each
+        // 16-byte load of a warp covers 512 consecutive bytes (no bank
+        // conflict); which thread holds an element does not matter, the
+        // elements of a range only need distinct slots of its run
         if (full) {
+            const ulonglong2* in2 = reinterpret_cast<const ulonglong2*>(in);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int j0 = 4 * (threadIdx.x + h * kPartThreads);
-                const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(in + j0);
-                const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(in + j0 + 2);
-                x[4 * h] = a.x; x[4 * h + 1] = a.y; x[4 * h + 2] = b.x; x[4 * h + 3] = b.y;
+            for (int q = 0; q < kPartEPT / 2; ++q) {
+                const ulonglong2 a = in2[threadIdx.x + q * kPartThreads];
+                x[2 * q] = a.x;
+                x[2 * q + 1] = a.y;
             }
 #pragma unroll
             for (int k = 0; k < kPartEPT; ++k) {
@@ -594,14 +598,10 @@ __global__ void __launch_bounds__(kPartThreads, kPartCtasPerSm)
             }
         } else {
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int j0 = 4 * (threadIdx.x + h * kPartThreads);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int j = j0 + q;
-                    r[4 * h + q] = j < cnt ? 0 : -1;
-                    x[4 * h + q] = j < have ? in[j] : (j < cnt ? src.raw1(e0 + j) : 0ULL);
-                }
+            for (int k = 0; k < kPartEPT; ++k) {
+                const int j = 2 * (threadIdx.x + (k >> 1) * kPartThreads) + (k & 1);
+                r[k] = j < cnt ? 0 : -1;
+                x[k] = j < have ? in[j] : (j < cnt ? src.raw1(e0 + j) : 0ULL);
             }
 #pragma unroll
             for (int k = 0; k < kPartEPT; ++k) hi_or |= r[k] == 0 ? (unsigned)(x[k] >> 32) : 0u;
