@@ -319,6 +319,37 @@ __device__ __forceinline__ unsigned bk_key24(unsigned k, int cbits) {
     return (((k >> 24) << cbits) | (k & 0xFFFFFFu)) & ((1u << (kBkShift + cbits)) - 1u);
 }
 
+// One stable scatter pass of the warp sort: positions 0 .. E-1 of src, 32 per
+// round, go to dst at base[digit] + (their rank among the round's lanes with
+// the same digit); base[] holds the running digit offsets.  Lanes holding
+// the same digit are found with one ballot per digit bit (the ALU pipe); a
+// match instruction per round (the ADU pipe) kept that pipe 66% busy and was
+// slower.  (Skipping the digit bits a pass cannot hold made no difference.)
+__device__ __forceinline__ void bk_rank_pass(const unsigned* src, unsigned* dst, int E, int shift, bool first,
+                                             unsigned* base, int lane, unsigned lt) {
+    for (int p0 = 0; p0 < E; p0 += 32) {
+        const int p = p0 + lane;
+        const bool ok = p < E;
+        const unsigned v = ok ? src[p] : 0u;
+        const unsigned d = (v >> shift) & 0xFFu;
+        unsigned peers = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const unsigned bb = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+            peers &= ((d >> b) & 1u) ? bb : ~bb;
+        }
+        unsigned at = 0;
+        if (ok) at = base[d];
+        __syncwarp();
+        if (ok) {
+            const unsigned before = peers & lt;
+            dst[at + __popc(before)] = first ? (((v >> 8) << kBkWarpIdxBits) | (unsigned)p) : v;
+            if (before == 0u) base[d] = at + __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_warp_kernel(
     const BkInst* __restrict__ inst, const BkItem* __restrict__ items, unsigned nitems, unsigned* cursor,
     const long long* __restrict__ bstart, const unsigned* __restrict__ bcount, const uint4* __restrict__ rec_in,
@@ -396,22 +427,7 @@ __global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_war
             }
             __syncwarp();
             const int shift = k == 0 ? 0 : 8 * k + 3;
-            for (int p0 = 0; p0 < E; p0 += 32) {
-                const int p = p0 + lane;
-                const bool ok = p < E;
-                const unsigned v = ok ? src[p] : 0u;
-                const unsigned d = ok ? ((v >> shift) & 0xFFu) : 0x100u;
-                const unsigned peers = __match_any_sync(0xffffffffu, d);
-                unsigned at = 0;
-                if (ok) at = base[d];
-                __syncwarp();
-                if (ok) {
-                    const unsigned before = peers & lt;
-                    dst[at + __popc(before)] = k == 0 ? (((v >> 8) << kBkWarpIdxBits) | (unsigned)p) : v;
-                    if (before == 0u) base[d] = at + __popc(peers);
-                }
-                __syncwarp();
-            }
+            bk_rank_pass(src, dst, E, shift, k == 0, base, lane, lt);
             unsigned* t = src;
             src = dst;
             dst = t;
@@ -420,7 +436,7 @@ __global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_war
         unsigned* const ord = src;
         unsigned* const key = dst;
         const unsigned cmask = (1u << cbits) - 1u;
-        constexpr int kG = 4;  // records in flight per lane
+        constexpr int kG = 8;  // records in flight per lane
         for (int p0 = lane; p0 < E; p0 += 32 * kG) {
             uint4 r[kG];
 #pragma unroll
