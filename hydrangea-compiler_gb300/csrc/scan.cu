@@ -391,8 +391,10 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
     __shared__ T sh_run[kScanTileP];  // the tile's values, then the running segment sums (padded)
     __shared__ unsigned sh_head[kScanTile / 32];
     __shared__ T sh_fold[kFoldBuf];
-    __shared__ T sh_wv[32];
-    __shared__ unsigned sh_wh;
+    __shared__ T sh_wv[32];             // each warp's inclusive (head seen, sum)
+    __shared__ unsigned sh_wh[32];
+    __shared__ T sh_wxv[32];            // each warp's exclusive prefix over the warps before it
+    __shared__ unsigned sh_wxh[32];
     __shared__ int64_t sh_sb, sh_se;
     __shared__ unsigned sh_tile_id;
     __shared__ T sh_carry;
@@ -432,6 +434,13 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
         bad |= !ok;
         if (ok && o - v0 < cnt) atomicOr(&sh_head[(o - v0) >> 5], 1u << ((o - v0) & 31));
     }
+    if (threadIdx.x == 0) {
+        // the end of the last segment, when values outside every segment
+        // follow it here, is a head too: every segment end is then followed
+        // by a head or by the end of the tile, which the running sums below rely on
+        const int64_t oe = offsets[nseg];
+        if (oe >= v0 && oe < v0 + cnt) atomicOr(&sh_head[(oe - v0) >> 5], 1u << ((oe - v0) & 31));
+    }
     // the segment open at the tile's start (begun in an earlier tile) ends at offsets[sb]
     const int64_t end_open = sb <= nseg ? offsets[sb] : 0;
     const bool open = tile > 0 && sb > 0 && end_open > v0;
@@ -444,44 +453,57 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
         }
         return;
     }
-    // segmented scan of the tile: thread t owns positions 8t .. 8t+7
+    // segmented scan of the tile: thread t owns positions 8t .. 8t+7.  Only
+    // segment ends (and the tile's last value) are read back, so each thread
+    // keeps its own segmented running sums (a head restarts the sum) and
+    // adds the carry from the positions before it once, at the one position
+    // that needs it: the last valid one before its first head.
     const int p0 = threadIdx.x * kScanIPT;
     const unsigned hb = (sh_head[p0 >> 5] >> (p0 & 31)) & 0xffu;
     T x[kScanIPT];
 #pragma unroll
     for (int j = 0; j < kScanIPT; ++j) x[j] = sh_run[scan_pad(p0 + j)];
-    bool h = hb != 0u;
-    T v = T(0);
 #pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) v = (hb >> j) & 1u ? x[j] : v + x[j];
-    // inclusive warp scan of (h, v), then exclusive across warps
+    for (int j = 1; j < kScanIPT; ++j)
+        if (!((hb >> j) & 1u)) x[j] = x[j - 1] + x[j];
+    const bool h = hb != 0u;
+    // inclusive warp scan of the threads' (head seen, sum) pairs
     bool hi_ = h;
-    T vi = v;
+    T vi = x[kScanIPT - 1];
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
         const bool hu = __shfl_up_sync(0xffffffffu, hi_, d);
         const T vu = __shfl_up_sync(0xffffffffu, vi, d);
         if (lane >= d) seg_combine(hi_, vi, hu, vu);
     }
-    const unsigned whead = __ballot_sync(0xffffffffu, h);
-    if (lane == 31) sh_wv[warp] = vi;
-    if (threadIdx.x == 0) sh_wh = 0u;
+    if (lane == 31) {
+        sh_wv[warp] = vi;
+        sh_wh[warp] = hi_;
+    }
     __syncthreads();
-    if (lane == 0 && whead) atomicOr(&sh_wh, 1u << warp);
-    __syncthreads();
-    bool he = false;
-    T ve = T(0);
-    {
-        // exclusive prefix over the warps before this one, in warp order
-        const unsigned wh = sh_wh;
-        for (int w = 0; w < warp; ++w) {
-            bool hw = (wh >> w) & 1u;
-            T vw = sh_wv[w];
-            seg_combine(hw, vw, he, ve);
-            he = hw;
-            ve = vw;
+    if (warp == 0) {
+        // exclusive scan over the warps' pairs, once (a fixed shuffle tree)
+        constexpr int kW = kScanT / 32;
+        bool hw = lane < kW ? sh_wh[lane] != 0u : false;
+        T vw = lane < kW ? sh_wv[lane] : T(0);
+#pragma unroll
+        for (int d = 1; d < kW; d <<= 1) {
+            const bool hu = __shfl_up_sync(0xffffffffu, hw, d);
+            const T vu = __shfl_up_sync(0xffffffffu, vw, d);
+            if (lane >= d) seg_combine(hw, vw, hu, vu);
         }
-        // then the lanes before this one within the warp
+        const bool hx = __shfl_up_sync(0xffffffffu, hw, 1);
+        const T vx = __shfl_up_sync(0xffffffffu, vw, 1);
+        if (lane < kW) {
+            sh_wxh[lane] = lane > 0 && hx;
+            sh_wxv[lane] = lane > 0 ? vx : T(0);
+        }
+    }
+    __syncthreads();
+    // this thread's exclusive carry: the warps before, then the lanes before
+    bool he = sh_wxh[warp] != 0u;
+    T ve = sh_wxv[warp];
+    {
         const bool hl = __shfl_up_sync(0xffffffffu, hi_, 1);
         const T vl = __shfl_up_sync(0xffffffffu, vi, 1);
         if (lane > 0) {
@@ -492,12 +514,17 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) segreduce_tile_kernel(
             ve = vv;
         }
     }
-    // running sums: the exclusive carry, then the thread's own positions
-    T r = ve;
+    {
+        const int lim = cnt - p0 < kScanIPT ? (cnt - p0 > 0 ? cnt - p0 : 0) : kScanIPT;
+        const int fh = hb ? __ffs(hb) - 1 : kScanIPT;
+        const int fix = (fh < lim ? fh : lim) - 1;  // -1: nothing before the first head
+        T sel = T(0);
 #pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) {
-        r = (hb >> j) & 1u ? x[j] : r + x[j];
-        sh_run[scan_pad(p0 + j)] = r;
+        for (int j = 0; j < kScanIPT; ++j)
+            if (j == fix) sel = x[j];
+        const T fixed = ve + sel;
+#pragma unroll
+        for (int j = 0; j < kScanIPT; ++j) sh_run[scan_pad(p0 + j)] = j == fix ? fixed : x[j];
     }
     const bool any_head = __syncthreads_or(h);
     // publish and look back (warp 0)
