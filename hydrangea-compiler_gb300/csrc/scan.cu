@@ -11,31 +11,37 @@
 // elements take their id from an atomic counter in launch order, so every
 // predecessor a tile waits on has already started; a tile publishes its
 // aggregate, a warp looks back 32 predecessors at a time, then publishes its
-// inclusive prefix.  Every spin is bounded (error bit, no hang).  int64 adds
-// wrap and commute, so the result is bit-identical to the serial C fold.
-// One read and one write per element: 16 B/element of HBM traffic.
+// inclusive prefix.  A tile's status is one 16-byte {flag, value} word
+// (TileWord), written and read whole, so a look-back window costs one memory
+// round trip.  Every spin is bounded (error bit, no hang).  int64 adds wrap
+// and commute, so the result is bit-identical to the serial C fold.  One
+// read and one write per element: 16 B/element of HBM traffic.
 //
-// float64: single-pass decoupled look-back with a deterministic combine.  A
-// tile publishes its aggregate, then looks back to the nearest predecessor
-// that has published an inclusive prefix and folds the aggregates in between
-// onto it left to right (lookback_fold).  Every inclusive prefix is made that
-// way, so each equals the left fold of all earlier tile aggregates onto init,
-// whatever the timing: results are run-to-run identical.  Within a tile the
-// order is fixed too (per-thread serial sums, a fixed shuffle tree).  A
-// parallel prefix cannot reproduce the serial fold's roundings; the tolerance
-// is |gpu - c| <= 1e-12 * prefix sum of |x| (stated in the tests).
+// float64: single pass, deterministic in two levels.  Within a block of 32
+// tiles a tile's prefix over its block-mates comes from a fixed warp scan of
+// their aggregates; across blocks the block totals are folded left to right
+// through the same kind of look-back (lookback_fold).  Every value is defined
+// by the data alone, not by timing: results are run-to-run identical.  Within
+// a tile the order is fixed too (per-thread serial sums, a fixed shuffle
+// tree).  A parallel prefix cannot reproduce the serial fold's roundings; the
+// tolerance is |gpu - c| <= 1e-12 * prefix sum of |x| (stated in the tests).
+//
+// Tiles pass through shared memory padded with one slot per 16 elements, so
+// the blocked (8 consecutive elements per thread) and striped accesses are
+// free of bank conflicts.
 //
 // segmented_reduce: tiles of 4096 values (not one warp per segment), so a long
 // segment is spread over many CTAs and many short ones share one.  A warp
-// finds the tile's segments with a 32-ary search of the offsets; a segmented
-// scan of the tile (head flags at segment starts, fixed shuffle tree) gives
-// every segment that ends in the tile its sum; the segment still open at the
-// tile's start gets its carry from the predecessors through the same
-// deterministic look-back (a tile that holds a segment start is an inclusive
-// prefix at once, so the look-back stops there).  One read of offsets and
-// values, one write of the sums.  Offsets that are not a non-decreasing
-// partition of [0, n_vals] are detected by the tiles and handed to a per-
-// segment kernel that gives the reference semantics (init, error reported).
+// finds the tile's segments with a 32-ary search of the offsets; each thread
+// keeps segmented running sums of its 8 values and takes the carry of the
+// positions before it (one fixed shuffle scan per warp, one over the warps)
+// where a segment end needs it; the segment still open at the tile's start
+// gets its carry from the predecessors through the deterministic look-back (a
+// tile that holds a segment start is an inclusive prefix at once, so the
+// look-back stops there).  One read of offsets and values, one write of the
+// sums.  Offsets that are not a non-decreasing partition of [0, n_vals] are
+// detected by the tiles and handed to a per-segment kernel that gives the
+// reference semantics (init, error reported).
 //
 // Reverse scans read and write index n-1-k for logical position k, exactly the
 // ix the reference's lowering computes.

@@ -660,7 +660,9 @@ __global__ void __launch_bounds__(kSpWarps * 32, kSpPerSm)
                     if (k0 + u < L) {
                         const unsigned c = (unsigned)cols[a + k0 + u];
                         v[u] = vals[a + k0 + u];
-                        if (c < ncols) xv[u] = x[c];
+                        // x is gathered through L2 only, so that the random
+                        // x lines do not evict the lanes' sequential row streams
+                        if (c < ncols) xv[u] = __ldcg(x + c);
                     }
                 }
 #pragma unroll

@@ -176,6 +176,27 @@ def test_segmented_reduce_values_outside_segments(hc, orc, dev):
     _check_segreduce(hc, orc, dev, offsets, int(offsets[-1]) + 12_345, seed=9)
 
 
+@pytest.mark.parametrize("tail", [0, 1, 3, 7, 8, 9, 4095, 4096, 4097])
+def test_segmented_reduce_ends_at_thread_and_tile_edges(hc, orc, dev, tail):
+    """Segment ends at every position class a tile's threads meet (8 values
+    per thread, 4096 per tile): ends on the last or first value of a thread,
+    one-value segments, runs of empty segments, and the last segment ending
+    `tail` values before n_vals (values outside every segment after it)."""
+    ends = []
+    pos = 0
+    for t in range(40):  # the first 40 threads of tiles 0 and 1, then a long one
+        for e in (8 * t + 7, 8 * t + 8, 8 * t + 9):
+            if e > pos:
+                ends += [e, e] if t % 5 == 0 else [e]  # some empty segments
+                pos = e
+    for e in (4095, 4096, 4097, 4103, 4104, 8191, 8192, 3 * 4096 + 5):
+        if e > pos:
+            ends.append(e)
+            pos = e
+    offsets = np.concatenate([[0], np.array(ends)]).astype(np.int64)
+    _check_segreduce(hc, orc, dev, offsets, int(offsets[-1]) + tail, seed=31 + tail)
+
+
 def test_segmented_reduce_empty_values_and_trailing_empties(hc, orc, dev):
     # no values at all: every segment is empty and yields init
     _check_segreduce(hc, orc, dev, np.zeros(1001, dtype=np.int64), 0, seed=1)
