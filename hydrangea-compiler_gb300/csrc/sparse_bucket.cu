@@ -436,47 +436,70 @@ __global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_war
         unsigned* const ord = src;
         unsigned* const key = dst;
         const unsigned cmask = (1u << cbits) - 1u;
-        constexpr int kG = 8;  // records in flight per lane
-        for (int p0 = lane; p0 < E; p0 += 32 * kG) {
+        // One pass over the sorted positions, 32 consecutive ones per warp step:
+        // gather each record for its key, CSR column and value, and find the
+        // row starts and any equal neighbouring keys from the neighbour's key
+        // (a shuffle; the step before hands over its last key).
+        unsigned* const rowb = base;  // [kBkRows + 1]
+        constexpr int kG = 8;         // records in flight per lane
+        unsigned prev_key = 0u;
+        int prev_row = -1;  // row of the position before the current step (-1: none)
+        bool dup = false;
+        for (int c0 = 0; c0 < E; c0 += 32 * kG) {
             uint4 r[kG];
 #pragma unroll
-            for (int u = 0; u < kG; ++u)
-                if (p0 + 32 * u < E) r[u] = rec_in[s0 + (ord[p0 + 32 * u] & (kBkWarpCap - 1))];
+            for (int u = 0; u < kG; ++u) {
+                const int p = c0 + 32 * u + lane;
+                if (p < E) r[u] = rec_in[s0 + (ord[p] & (kBkWarpCap - 1))];
+            }
 #pragma unroll
             for (int u = 0; u < kG; ++u) {
-                const int p = p0 + 32 * u;
-                if (p < E) {
-                    const unsigned k24 = bk_key24(r[u].x, cbits);
+                const int p = c0 + 32 * u + lane;
+                const bool in = p < E;
+                unsigned k24 = 0u;
+                if (in) {
+                    k24 = bk_key24(r[u].x, cbits);
                     key[p] = k24;
                     I.csr_cols[e0 + p] = (int)(k24 & cmask);
                     I.csr_vals[e0 + p] = bk_rec_val(r[u]);
                 }
+                const int row = in ? (int)(k24 >> cbits) : kBkRows;
+                const unsigned kup = __shfl_up_sync(0xffffffffu, k24, 1);
+                const int rup = __shfl_up_sync(0xffffffffu, row, 1);
+                const unsigned kprev = lane == 0 ? prev_key : kup;
+                const int rprev = lane == 0 ? prev_row : rup;
+                if (in) {
+                    for (int rr = rprev + 1; rr <= row && rr < kBkRows; ++rr) rowb[rr] = (unsigned)p;
+                    dup |= p > 0 && kprev == k24;
+                }
+                prev_key = __shfl_sync(0xffffffffu, k24, 31);
+                prev_row = __shfl_sync(0xffffffffu, row, 31);
             }
         }
         __syncwarp();
-        unsigned* const rowb = base;  // [kBkRows + 1]
-        for (int p = lane; p <= E; p += 32) {
-            const int rp = p == 0 ? -1 : (int)(key[p - 1] >> cbits);
-            const int rc = p == E ? kBkRows : (int)(key[p] >> cbits);
-            for (int r = rp + 1; r <= rc && r < kBkRows; ++r) rowb[r] = (unsigned)p;
+        {  // rows after the last entry's row (every row when the bucket is empty) start at E
+            const int last_row = E > 0 ? (int)(key[E - 1] >> cbits) : -1;
+            for (int rr = last_row + 1 + lane; rr <= kBkRows; rr += 32) rowb[rr] = (unsigned)E;
         }
-        if (lane == 0) rowb[kBkRows] = (unsigned)E;
         // equal (row, col) keys in COO-position order (duplicates are rare)
-        for (int p = lane; p + 1 < E; p += 32) {
-            if (key[p + 1] != key[p] || (p > 0 && key[p - 1] == key[p])) continue;
-            int q = p + 2;
-            while (q < E && key[q] == key[p]) ++q;
-            for (int i = p + 1; i < q; ++i) {
-                const unsigned v = ord[i];
-                const unsigned kv = rec_in[s0 + (v & (kBkWarpCap - 1))].y;  // COO position
-                int j = i - 1;
-                while (j >= p && rec_in[s0 + (ord[j] & (kBkWarpCap - 1))].y > kv) {
-                    ord[j + 1] = ord[j];
-                    --j;
+        if (__any_sync(0xffffffffu, dup)) {
+            for (int p = lane; p + 1 < E; p += 32) {
+                if (key[p + 1] != key[p] || (p > 0 && key[p - 1] == key[p])) continue;
+                int q = p + 2;
+                while (q < E && key[q] == key[p]) ++q;
+                for (int i = p + 1; i < q; ++i) {
+                    const unsigned v = ord[i];
+                    const unsigned kv = rec_in[s0 + (v & (kBkWarpCap - 1))].y;  // COO position
+                    int j = i - 1;
+                    while (j >= p && rec_in[s0 + (ord[j] & (kBkWarpCap - 1))].y > kv) {
+                        ord[j + 1] = ord[j];
+                        --j;
+                    }
+                    ord[j + 1] = v;
                 }
-                ord[j + 1] = v;
+                for (int i = p; i < q; ++i)
+                    I.csr_vals[e0 + i] = bk_rec_val(rec_in[s0 + (ord[i] & (kBkWarpCap - 1))]);
             }
-            for (int i = p; i < q; ++i) I.csr_vals[e0 + i] = bk_rec_val(rec_in[s0 + (ord[i] & (kBkWarpCap - 1))]);
         }
         __syncwarp();
         for (int r = lane; r <= nr; r += 32) {
