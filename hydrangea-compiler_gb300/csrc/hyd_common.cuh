@@ -211,8 +211,6 @@ __device__ __forceinline__ void bulk_load_1d(unsigned dst, const void* src, unsi
 // ---- decoupled look-back: tile status words and the bounded window wait ------
 constexpr unsigned kSpinLimit = 1u << 22;  // polls before a look-back gives up
 
-__device__ __forceinline__ unsigned ld_volatile_u32(const unsigned* p) { return *(volatile const unsigned*)p; }
-
 // One tile's status: flag 0 = nothing published, 1 = `bits` hold the tile's
 // aggregate, 2 = `bits` hold the inclusive prefix through the tile.  A status
 // is written and read as one 16-byte access, so a reader gets a flag together
