@@ -92,7 +92,58 @@ static std::string map_source(const std::string& body, int nin, bool i64) {
          "  " + A + " acc = 0;\n"
          "  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
          "  const long long nt = (long long)gridDim.x * blockDim.x;\n"
-         "  if (vec) {\n"
+         "  if (vec == 2) {\n"
+         "    const long long nq = n >> 2;\n"
+         "    long long q = t;\n"
+         "    for (; q < nq; q += 2 * nt) {\n"
+         "      const bool two = q + nt < nq;\n";
+    // 32-byte vectors, two per lane per step (8 elements), all loads first
+    const std::string LD = i64 ? "ld.global.nc.L1::no_allocate.v4.u64" : "ld.global.nc.L1::no_allocate.v4.f64";
+    const std::string ST = i64 ? "st.global.v4.u64" : "st.global.v4.f64";
+    const std::string RC = i64 ? "l" : "d";
+    for (int k = 0; k < kMapMaxInputs; ++k) {
+        const std::string ks = std::to_string(k);
+        s += "      " + T + " a" + ks + "[8];\n";
+        if (k < nin) {
+            for (int h = 0; h < 2; ++h) {
+                const std::string hs = std::to_string(h);
+                s += std::string("      ") + (h ? "if (two) " : "") + "asm volatile(\"" + LD +
+                     " {%0,%1,%2,%3}, [%4];\" : \"=" + RC + "\"(a" + ks + "[" + std::to_string(4 * h) + "]), \"=" + RC +
+                     "\"(a" + ks + "[" + std::to_string(4 * h + 1) + "]), \"=" + RC + "\"(a" + ks + "[" +
+                     std::to_string(4 * h + 2) + "]), \"=" + RC + "\"(a" + ks + "[" + std::to_string(4 * h + 3) +
+                     "]) : \"l\"(p" + ks + " + 4 * (q + " + hs + " * nt)));\n";
+                if (h) s += "      else { a" + ks + "[4] = a" + ks + "[5] = a" + ks + "[6] = a" + ks + "[7] = " + zero + "; }\n";
+            }
+        } else {
+            s += "      for (int u = 0; u < 8; ++u) a" + ks + "[u] = " + zero + ";\n";
+        }
+    }
+    s += "      " + T + " w[8];\n"
+         "      #pragma unroll\n"
+         "      for (int u = 0; u < 8; ++u) w[u] = hyd_elem(4 * (q + (u >> 2) * nt) + (u & 3)";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += ", a" + std::to_string(k) + "[u]";
+    s += ");\n"
+         "      if (out) {\n"
+         "        asm volatile(\"" + ST + " [%0], {%1,%2,%3,%4};\" :: \"l\"(out + 4 * q), \"" + RC + "\"(w[0]), \"" +
+         RC + "\"(w[1]), \"" + RC + "\"(w[2]), \"" + RC + "\"(w[3]) : \"memory\");\n"
+         "        if (two) asm volatile(\"" + ST + " [%0], {%1,%2,%3,%4};\" :: \"l\"(out + 4 * (q + nt)), \"" + RC +
+         "\"(w[4]), \"" + RC + "\"(w[5]), \"" + RC + "\"(w[6]), \"" + RC + "\"(w[7]) : \"memory\");\n"
+         "      }\n"
+         "      #pragma unroll\n"
+         "      for (int u = 0; u < 4; ++u) acc += (" + A + ")w[u];\n"
+         "      if (two) {\n"
+         "        #pragma unroll\n"
+         "        for (int u = 4; u < 8; ++u) acc += (" + A + ")w[u];\n"
+         "      }\n"
+         "    }\n"
+         "    for (long long i = 4 * nq + t; i < n; i += nt) {\n"
+         "      const " + T + " v = hyd_elem(i";
+    for (int k = 0; k < kMapMaxInputs; ++k) s += k < nin ? ", p" + std::to_string(k) + "[i]" : ", " + zero;
+    s += ");\n"
+         "      if (out) out[i] = v;\n"
+         "      acc += (" + A + ")v;\n"
+         "    }\n"
+         "  } else if (vec) {\n"
          "    const long long np = n >> 1;\n"
          "    for (long long q = t; q < np; q += nt) {\n"
          "      const long long i = 2 * q;\n";
@@ -231,11 +282,16 @@ static int map_launch(const char* body, const T* const* inputs, int ninputs, int
         if (sum) HYD_CUDA_TRY(cudaMemsetAsync(sum, 0, sizeof(T), s));
         return HYD_CUDA_OK;
     }
+    // 2: every pointer 32-byte aligned (256-bit loads and stores); 1: 16-byte
+    // aligned (128-bit); 0: scalar.  A null `out` counts as aligned, so a
+    // reduction alone takes the same path, and gives the same bits, as with out.
     bool vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    bool vec32 = (reinterpret_cast<uintptr_t>(out) & 31) == 0;
     const T* p[kMapMaxInputs] = {nullptr};
     for (int k = 0; k < ninputs; ++k) {
         p[k] = inputs[k];
         vec = vec && (reinterpret_cast<uintptr_t>(p[k]) & 15) == 0;
+        vec32 = vec32 && (reinterpret_cast<uintptr_t>(p[k]) & 31) == 0;
     }
     const int64_t pairs = (n + 1) / 2;
     int64_t grid = (pairs + kMapThreads - 1) / kMapThreads;
@@ -247,7 +303,7 @@ static int map_launch(const char* body, const T* const* inputs, int ninputs, int
     unsigned* counter = counters + 200;  // reset by the kernel's last block
     void* partials = scratch;
     long long nn = n;
-    int v = vec ? 1 : 0;
+    int v = vec32 ? 2 : (vec ? 1 : 0);
     void* args[kMapMaxInputs + 6];
     for (int k = 0; k < kMapMaxInputs; ++k) args[k] = &p[k];
     args[kMapMaxInputs + 0] = &nn;
