@@ -14,8 +14,9 @@
 //  2. one exclusive scan (the decoupled look-back int64 scan) turns the counts
 //     into each (digit, tile)'s first output position, and
 //  3. a stable scatter: each warp ranks its 256 contiguous elements in 8 rounds
-//     of 32 with __match_any_sync (lanes in element order, running counts per
-//     (warp, digit) in shared memory), so equal digits keep input order.
+//     of 32 among the lanes holding the same digit (one ballot per digit bit;
+//     lanes in element order, running counts per (warp, digit) in shared
+//     memory), so equal digits keep input order.
 // Keys travel with their original index; the first pass generates the
 // indices, the last pass writes only the permutation.
 #include "hyd_common.cuh"
@@ -77,15 +78,20 @@ __global__ void __launch_bounds__(kSortT) radix_scatter_kernel(const long long* 
         k[r] = ok ? keys_in[e] : 0;
         v[r] = ok ? (kFirst ? (long long)e : vals_in[e]) : 0;
         dig[r] = ok ? digit_of(k[r], shift) : 0x100u;  // 0x100: past the end
-        const unsigned active = __ballot_sync(0xffffffffu, ok);
-        unsigned peers = __match_any_sync(0xffffffffu, dig[r]);
+        // the lanes holding the same digit: one ballot per digit bit (the ALU
+        // pipe) rather than a match instruction (the ADU pipe, which binds)
+        unsigned peers = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const unsigned bb = __ballot_sync(0xffffffffu, (dig[r] >> b) & 1u);
+            peers &= ((dig[r] >> b) & 1u) ? bb : ~bb;
+        }
         unsigned prior = 0;
         if (ok) prior = wcount[warp][dig[r]];
         __syncwarp();
         rank[r] = prior + __popc(peers & lt);
         if (ok && (peers & lt) == 0u) wcount[warp][dig[r]] = prior + __popc(peers);
         __syncwarp();
-        (void)active;
     }
     __syncthreads();
     // exclusive prefix over warps for each digit (warp order = element order)

@@ -294,10 +294,12 @@ __device__ __forceinline__ void bk_order_equal_keys(const unsigned* key, IdxT* p
 //    (key24 >> 8) << 11 | index; later passes move that word, whose bits
 //    8k + 3 ... hold digit k, so one 32-bit word per entry carries both the
 //    remaining key and the entry index;
-//  * each pass ranks 32 positions per round with __match_any_sync, so equal
-//    digits keep their order;
+//  * each pass ranks 32 positions per round among the lanes holding the same
+//    digit (bk_rank_pass), so equal digits keep their order;
 //  * after the sort every slot's record is gathered once for its full key,
-//    CSR column and value; runs of equal keys are then put in COO order.
+//    CSR column and value, 32 consecutive slots per step, which also gives
+//    the row starts and any equal neighbouring keys; runs of equal keys are
+//    then put in COO order.
 // Row starts come from the masked keys, which are sorted on every bit they
 // have whatever the records hold, so every row range stays inside [0, E].
 // Buckets above kBkWarpCap entries, or of instances with more than 2^18
