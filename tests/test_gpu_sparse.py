@@ -240,3 +240,29 @@ def test_batched_out_of_range_entry_reported(hc, orc, dev, pipeline, bad, monkey
     hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
     assert hc.device_check() == hc.ERR_BOUNDS
     assert hc.device_check() == hc.OK
+
+
+@pytest.mark.parametrize("pipeline", ["bucketed", "rows"])
+def test_batched_row_above_256_entries_reported(hc, orc, dev, pipeline, monkeypatch):
+    """A row with more than 256 entries is outside the batched pipeline's
+    contract: both forms report it through hyd_cuda_check, and the device
+    stays usable for the next call."""
+    if pipeline == "rows":
+        monkeypatch.setenv("HYD_CUDA_BATCH_PIPELINE", "rows")
+    rng = np.random.default_rng(17)
+    n, ncols, long_len = 200, 4096, 300
+    r = np.concatenate([np.full(long_len, 7), rng.integers(0, n, 2000)])
+    c = np.concatenate([rng.permutation(ncols)[:long_len], rng.integers(0, ncols, 2000)])
+    desc = np.array([(n, ncols, len(r))], dtype=np.int64)
+    rows = torch.from_numpy(r.astype(np.int32)).to(dev)
+    cols = torch.from_numpy(c.astype(np.int32)).to(dev)
+    vals = torch.from_numpy(rng.uniform(-1, 1, len(r))).to(dev)
+    x = torch.from_numpy(rng.uniform(-1, 1, ncols)).to(dev)
+    hc.batched_coo_csr_spmv(desc, rows, cols, vals, x)
+    assert hc.device_check() == hc.ERR_BOUNDS
+    assert hc.device_check() == hc.OK
+    # a batch within the contract right after gives the oracle's results
+    desc2, rows2, cols2, vals2, x2 = hc.synth_coo_batch(2, seed0=11, min_log2=8, max_log2=10)
+    out = hc.batched_coo_csr_spmv(desc2, rows2, cols2, vals2, x2)
+    hc.check(hc.device_check())
+    _check_batch(hc, orc, desc2, rows2, cols2, vals2, x2, *out)
