@@ -74,6 +74,36 @@ def test_scan_f64_tolerance(hc, orc, dev, n, variant):
     assert torch.equal(out, out2)  # run-to-run reproducible
 
 
+def test_scans_at_the_benchmark_size(hc, orc, dev):
+    """Both scans at the benchmarked 2^27 elements (32768 tiles, 1024 blocks of
+    the float64 scan's two-level fold): int64 bit-exact against the oracle's
+    serial fold, float64 within the tolerance and identical over runs, forward
+    exclusive (the benchmark's form) and reverse inclusive."""
+    n = 1 << 27
+    xi = _i64(hc, n, dev, seed=41)
+    hi = xi.cpu().numpy()
+    xf = torch.empty(n, dtype=torch.float64, device=dev)
+    hc.fill_uniform_f64(xf, 41, -1.0, 1.0)
+    hf = xf.cpu().numpy()
+    for rev, inc in ((False, False), (True, True)):
+        out = torch.empty_like(xi)
+        hc.scan(xi, out, 3, rev, inc)
+        hc.check(hc.device_check())
+        assert np.array_equal(out.cpu().numpy(), orc.scan_i64(hi, 3, rev, inc))
+        del out
+        outs = []
+        for _ in range(2):
+            o = torch.empty_like(xf)
+            hc.scan(xf, o, 0.5, rev, inc)
+            outs.append(o)
+        hc.check(hc.device_check())
+        ref = orc.scan_f64(hf, 0.5, rev, inc)
+        bound = orc.scan_f64(np.abs(hf), 0.5, rev, inc)
+        assert np.all(np.abs(outs[0].cpu().numpy() - ref) <= 1e-12 * np.maximum(bound, 1.0))
+        assert torch.equal(outs[0], outs[1])
+        del outs
+
+
 @pytest.mark.parametrize("nseg", [0, 1, 5, 1000, 100_000])
 def test_segmented_reduce(hc, orc, dev, nseg):
     rng = np.random.default_rng(nseg)
