@@ -104,6 +104,23 @@ def test_scans_at_the_benchmark_size(hc, orc, dev):
         del outs
 
 
+def test_segmented_reduce_at_the_benchmark_size(hc, orc, dev):
+    """The benchmarked segmented reduce: 2^27 float64 and int64 values, segment
+    lengths floor(2^U(0,16)) (seed 43, about 22,700 segments, the longest
+    near 2^16): int64 bit-exact, float64 within the tolerance of the serial
+    sums and identical over runs."""
+    n = 1 << 27
+    rng = np.random.default_rng(43)
+    lens = np.floor(2.0 ** rng.uniform(0, 16, size=n // 1000)).astype(np.int64)
+    cum = np.cumsum(lens)
+    k = int(np.searchsorted(cum, n))
+    lens = lens[:k + 1]
+    lens[-1] -= int(cum[k] - n)
+    offsets = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    offsets[-1] = n
+    _check_segreduce(hc, orc, dev, offsets, n, seed=43)
+
+
 @pytest.mark.parametrize("nseg", [0, 1, 5, 1000, 100_000])
 def test_segmented_reduce(hc, orc, dev, nseg):
     rng = np.random.default_rng(nseg)
