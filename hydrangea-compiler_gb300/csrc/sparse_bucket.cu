@@ -282,7 +282,7 @@ __device__ __forceinline__ void bk_order_equal_keys(const unsigned* key, IdxT* p
 }
 
 // One warp per bucket: a warp sorts its own bucket with no block barrier, so
-// twelve independent buckets are in flight per SM.  (A CTA per ~800-entry
+// fifteen independent buckets are in flight per SM.  (A CTA per ~800-entry
 // bucket pays its fixed work -- zeroing and scanning a counter set per warp,
 // five block barriers per radix pass -- once per bucket.)
 //  * key24 = row_in_bucket << cbits | col, kept to its 6 + cbits <= 24 bits,
@@ -302,17 +302,20 @@ __device__ __forceinline__ void bk_order_equal_keys(const unsigned* key, IdxT* p
 //    then put in COO order.
 // Row starts come from the masked keys, which are sorted on every bit they
 // have whatever the records hold, so every row range stays inside [0, E].
-// Buckets above kBkWarpCap entries, or of instances with more than 2^18
+// The pipeline runs it with room for 1536 entries per warp (fifteen warps per
+// SM; 0.5% of the workload's buckets are larger).  Buckets above kCap, or of
+// instances with more than 2^18
 // columns, go to `overflow` (the block-wide kernel below).
-constexpr int kBkWarpCap = 2048;
-constexpr int kBkWarpIdxBits = 11;  // log2(kBkWarpCap)
+constexpr int kBkWarpIdxBits = 11;   // entry index bits: buckets of at most 2048 entries
+constexpr unsigned kBkWarpIdxMask = (1u << kBkWarpIdxBits) - 1u;
 constexpr int kBkWarpMaxCbits = 24 - kBkShift;
-constexpr int kBkWarpWarps = 4;  // warps (buckets) per CTA
 constexpr int kBkWarpPerSm = 3;  // resident CTAs per SM
 // per warp (32-bit words): two key buffers, packed digit counts of three
 // passes, the running digit bases (later the row starts)
-constexpr int kBkWarpWords = 2 * kBkWarpCap + 3 * 128 + 256;
-constexpr size_t kBkWarpSmem = (size_t)kBkWarpWarps * kBkWarpWords * 4;
+template <int kCap>
+__host__ __device__ constexpr int bk_warp_words() { return 2 * kCap + 3 * 128 + 256; }
+template <int kCap, int kWarps>
+constexpr size_t bk_warp_smem() { return (size_t)kWarps * bk_warp_words<kCap>() * 4; }
 
 // The sort key of a record: row_in_bucket << cbits | col, kept to its 6 + cbits
 // bits (which change nothing for a valid entry, and keep every key's row
@@ -352,15 +355,20 @@ __device__ __forceinline__ void bk_rank_pass(const unsigned* src, unsigned* dst,
     }
 }
 
-__global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_warp_kernel(
-    const BkInst* __restrict__ inst, const BkItem* __restrict__ items, unsigned nitems, unsigned* cursor,
+template <int kCap, int kWarps>
+__global__ void __launch_bounds__(kWarps * 32, kBkWarpPerSm) bk_bucket_warp_kernel(
+    const BkInst* __restrict__ inst, const BkItem* __restrict__ items, unsigned nitems_host,
+    const unsigned* nitems_dev, unsigned* cursor,
     const long long* __restrict__ bstart, const unsigned* __restrict__ bcount, const uint4* __restrict__ rec_in,
     BkItem* __restrict__ overflow, unsigned* overflow_count, unsigned* err) {
     extern __shared__ __align__(16) unsigned bkw_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned* const a = bkw_smem + (size_t)warp * kBkWarpWords;
-    unsigned* const b = a + kBkWarpCap;
-    unsigned* const hist = b + kBkWarpCap;  // [3][128]
+    static_assert(kCap <= (1 << kBkWarpIdxBits), "entry indices must fit their field");
+    unsigned* const a = bkw_smem + (size_t)warp * bk_warp_words<kCap>();
+    unsigned* const b = a + kCap;
+    unsigned* const hist = b + kCap;  // [3][128]
+    // the item count: given, or read from device memory (a list another kernel filled)
+    const unsigned nitems = nitems_dev ? *(volatile const unsigned*)nitems_dev : nitems_host;
     unsigned* const base = hist + 3 * 128;  // [256]; row starts [65] after the sort
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
@@ -375,7 +383,7 @@ __global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_war
         const int E = (int)bcount[gb];
         int cbits = 0;
         while ((1LL << cbits) < I.ncols) ++cbits;
-        if (E > kBkWarpCap || cbits > kBkWarpMaxCbits) {
+        if (E > kCap || cbits > kBkWarpMaxCbits) {
             if (lane == 0) overflow[atomicAdd(overflow_count, 1u)] = w;
             continue;  // warp-uniform
         }
@@ -452,7 +460,7 @@ __global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_war
 #pragma unroll
             for (int u = 0; u < kG; ++u) {
                 const int p = c0 + 32 * u + lane;
-                if (p < E) r[u] = rec_in[s0 + (ord[p] & (kBkWarpCap - 1))];
+                if (p < E) r[u] = rec_in[s0 + (ord[p] & kBkWarpIdxMask)];
             }
 #pragma unroll
             for (int u = 0; u < kG; ++u) {
@@ -491,16 +499,16 @@ __global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_war
                 while (q < E && key[q] == key[p]) ++q;
                 for (int i = p + 1; i < q; ++i) {
                     const unsigned v = ord[i];
-                    const unsigned kv = rec_in[s0 + (v & (kBkWarpCap - 1))].y;  // COO position
+                    const unsigned kv = rec_in[s0 + (v & kBkWarpIdxMask)].y;  // COO position
                     int j = i - 1;
-                    while (j >= p && rec_in[s0 + (ord[j] & (kBkWarpCap - 1))].y > kv) {
+                    while (j >= p && rec_in[s0 + (ord[j] & kBkWarpIdxMask)].y > kv) {
                         ord[j + 1] = ord[j];
                         --j;
                     }
                     ord[j + 1] = v;
                 }
                 for (int i = p; i < q; ++i)
-                    I.csr_vals[e0 + i] = bk_rec_val(rec_in[s0 + (ord[i] & (kBkWarpCap - 1))]);
+                    I.csr_vals[e0 + i] = bk_rec_val(rec_in[s0 + (ord[i] & kBkWarpIdxMask)]);
             }
         }
         __syncwarp();
@@ -514,7 +522,7 @@ __global__ void __launch_bounds__(kBkWarpWarps * 32, kBkWarpPerSm) bk_bucket_war
 
 // Large buckets (up to 64 rows x 256): one CTA sorts the bucket's keys with a
 // block-wide bitonic network in shared memory.  Reads its item count from
-// device memory (filled by the fast kernel).
+// device memory (filled by the warp sort).
 constexpr size_t kBkSmem = (size_t)kBkCap * 6 + 1024;
 
 __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __restrict__ inst,
@@ -759,7 +767,7 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     long long* wide = reinterpret_cast<long long*>(take(wide_b));
     long long* bstart = reinterpret_cast<long long*>(take(wide_b));
     uint4* recs = reinterpret_cast<uint4*>(take(2 * vals_b));  // (key, COO position, value) per entry
-    BkItem* overflow = reinterpret_cast<BkItem*>(take(bk_b));
+    BkItem* overflow = reinterpret_cast<BkItem*>(take(bk_b));  // buckets above 1536 entries
     BkItem* d_chunks = reinterpret_cast<BkItem*>(take(ch_b));
     unsigned* cursors = reinterpret_cast<unsigned*>(take(256));
     // only the instance table crosses from the host; the work lists are
@@ -795,10 +803,17 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
                                                              bfill, recs, d->d_err);
         HYD_TRY(launch_check("bk_split"));
     }
-    HYD_TRY(configure_kernel((const void*)bk_bucket_warp_kernel, d, false));
-    bk_bucket_warp_kernel<<<(unsigned)(d->sm_count * kBkWarpPerSm), kBkWarpWarps * 32, kBkWarpSmem, s>>>(
-        d_inst, d_bk, (unsigned)n_buckets, cursors + 2, bstart, bcount, recs, overflow, cursors + 4, d->d_err);
-    HYD_TRY(launch_check("bk_bucket_warp"));
+    // cursors: 2 the warp sort, 3 the block-wide kernel, 4 the overflow count.
+    // (A second warp run over the overflow, with room for 2048 entries, took
+    // 0.33 ms against the block-wide kernel's 0.21.)
+    {
+        auto k1 = bk_bucket_warp_kernel<1536, 5>;
+        HYD_TRY(configure_kernel((const void*)k1, d, false));
+        k1<<<(unsigned)(d->sm_count * kBkWarpPerSm), 5 * 32, bk_warp_smem<1536, 5>(), s>>>(
+            d_inst, d_bk, (unsigned)n_buckets, nullptr, cursors + 2, bstart, bcount, recs, overflow, cursors + 4,
+            d->d_err);
+        HYD_TRY(launch_check("bk_bucket_warp"));
+    }
     HYD_TRY(configure_kernel((const void*)bk_bucket_kernel, d, false));
     bk_bucket_kernel<<<grid, kBkThreads, kBkSmem, s>>>(d_inst, overflow, cursors + 4, cursors + 3, bstart, bcount,
                                                        recs, d->d_err);
