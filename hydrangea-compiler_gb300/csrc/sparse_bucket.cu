@@ -3,9 +3,10 @@
 // Same contract as batch_pipeline in sparse.cu (per instance: CSR of the
 // entries sorted by (row, col), y = A x), organised so that no stage walks
 // rows one dependent memory chain at a time:
-//  1. count   per (instance, 8192-entry tile): a shared-memory histogram of
-//             64-row buckets (row >> 6), flushed with one global red per
-//             non-empty bucket;
+//  1. count   per CTA, a contiguous range of (instance, 8192-entry tile)
+//             items: a shared-memory histogram of 64-row buckets (row >> 6),
+//             flushed with one global red per non-empty bucket when the
+//             instance changes;
 //  2. scan    exclusive scan of the ~4e5 bucket counts gives every bucket's
 //             first slot (instances are contiguous, so bucket starts are also
 //             each instance's entry offsets);
@@ -77,21 +78,49 @@ __device__ __forceinline__ bool bk_next(unsigned* cursor, unsigned nitems, unsig
     return item < nitems;
 }
 
-// Stage 1.
-__global__ void __launch_bounds__(kBkThreads) bk_count_kernel(const BkInst* __restrict__ inst,
+// Stage 1.  Each CTA counts a contiguous range of the tile list (the tiles of
+// an instance are consecutive there), keeping its shared-memory bucket counts
+// across the tiles of one instance and flushing them with one global red per
+// non-empty bucket when the instance changes.  A flush per tile issued about
+// one red per two entries for the largest instances, and the L2 atomics bound
+// the kernel.  The counts are zero whenever they are not in use (the flush
+// zeroes what it reads).
+constexpr int kCountPerSm = 4;
+__global__ void __launch_bounds__(kBkThreads, kCountPerSm) bk_count_kernel(const BkInst* __restrict__ inst,
                                                               const BkItem* __restrict__ items, unsigned nitems,
-                                                              unsigned* cursor, unsigned* __restrict__ bcount,
-                                                              unsigned* err) {
+                                                              unsigned* __restrict__ bcount, unsigned* err) {
     __shared__ unsigned hist[kMaxSmemBuckets];
-    unsigned it;
+    for (int b = threadIdx.x; b < kMaxSmemBuckets; b += kBkThreads) hist[b] = 0u;
+    const unsigned per = (nitems + gridDim.x - 1) / gridDim.x;
+    const unsigned i0 = blockIdx.x * per;
+    const unsigned i1 = i0 + per < nitems ? i0 + per : nitems;
+    int cur = -1;
+    long long cur_base = 0;
+    int cur_nb = 0;
     bool bad = false;
-    while (bk_next(cursor, nitems, it)) {
+    auto flush = [&]() {
+        if (cur >= 0 && cur_nb <= kMaxSmemBuckets)
+            for (int b = threadIdx.x; b < cur_nb; b += kBkThreads) {
+                const unsigned c = hist[b];
+                if (c) {
+                    atomicAdd(&bcount[cur_base + b], c);
+                    hist[b] = 0u;
+                }
+            }
+    };
+    __syncthreads();
+    for (unsigned it = i0; it < i1; ++it) {
         const BkItem w = items[it];
         const BkInst I = inst[w.inst];
-        const bool smem = I.nbuckets <= kMaxSmemBuckets;
-        if (smem)
-            for (int b = threadIdx.x; b < I.nbuckets; b += kBkThreads) hist[b] = 0u;
-        __syncthreads();
+        if (w.inst != cur) {
+            __syncthreads();  // the counting of the previous tile is complete
+            flush();
+            cur = w.inst;
+            cur_base = I.bucket_base;
+            cur_nb = (int)I.nbuckets;
+            __syncthreads();  // the flush has read and zeroed every count
+        }
+        const bool smem = cur_nb <= kMaxSmemBuckets;
         const long long t0 = (long long)w.tile * kTileEntries;
         const long long t1 = t0 + kTileEntries < I.nnz ? t0 + kTileEntries : I.nnz;
         // all of this thread's rows first (read-only loads, all in flight at
@@ -114,12 +143,9 @@ __global__ void __launch_bounds__(kBkThreads) bk_count_kernel(const BkInst* __re
             if (smem) atomicAdd(&hist[r >> kBkShift], 1u);
             else atomicAdd(&bcount[I.bucket_base + (r >> kBkShift)], 1u);
         }
-        __syncthreads();
-        if (smem)
-            for (int b = threadIdx.x; b < I.nbuckets; b += kBkThreads)
-                if (hist[b]) atomicAdd(&bcount[I.bucket_base + b], hist[b]);
-        __syncthreads();
     }
+    __syncthreads();
+    flush();
     if (bad) raise_error(err, ERRBIT_BOUNDS);
 }
 
@@ -790,8 +816,9 @@ int batch_pipeline_bucketed(std::vector<BatchInst>& bi, const char* key, cudaStr
     HYD_CUDA_TRY(cudaMemsetAsync(cursors, 0, 64, s));
     const unsigned grid = (unsigned)(d->sm_count * 2);
     if (n_tiles) {
-        bk_count_kernel<<<grid, kBkThreads, 0, s>>>(d_inst, d_tiles, (unsigned)n_tiles, cursors + 0, bcount,
-                                                    d->d_err);
+        bk_count_kernel<<<(unsigned)(d->sm_count * kCountPerSm), kBkThreads, 0, s>>>(d_inst, d_tiles,
+                                                                                   (unsigned)n_tiles, bcount,
+                                                                                   d->d_err);
         HYD_TRY(launch_check("bk_count"));
     }
     bk_widen_kernel<<<grid, 256, 0, s>>>(bcount, wide, nb_total);
