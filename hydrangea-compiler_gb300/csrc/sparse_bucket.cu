@@ -630,12 +630,11 @@ __global__ void __launch_bounds__(kBkThreads) bk_bucket_kernel(const BkInst* __r
 // the 32 rows of a warp instruction have similar lengths: a warp takes a
 // 256-row chunk of one instance, counting-sorts its rows by length (256 bins,
 // lengths above 255 share the last) in shared memory, and gives each lane one
-// row of every group of 32 consecutive rows in that order.  Loads run kSpAhead
-// entries ahead of the (in-order) chain.  Rows above 256 entries are outside
-// the contract and reported.
+// row of every group of 32 consecutive rows in that order.  A lane reads its
+// row 4 entries at a time with 16-byte loads, ahead of the (in-order) chain.
+// Rows above 256 entries are outside the contract and reported.
 constexpr int kSpWarps = 8;
 constexpr int kSpPerSm = 4;
-constexpr int kSpAhead = 4;
 struct BkSpSmem {
     unsigned cnt[256];
     unsigned start[kSpRows];
@@ -709,25 +708,40 @@ __global__ void __launch_bounds__(kSpWarps * 32, kSpPerSm)
             const int i = sm.order[g];
             const long long a = sm.start[i];
             const int L = sm.len[i];
+            const int* __restrict__ rc = cols + a;
+            const double* __restrict__ rv = vals + a;
             double acc = 0.0;
-            for (int k0 = 0; k0 < L; k0 += kSpAhead) {
-                double v[kSpAhead], xv[kSpAhead];
-#pragma unroll
-                for (int u = 0; u < kSpAhead; ++u) {
-                    v[u] = 0.0;
-                    xv[u] = 0.0;
-                    if (k0 + u < L) {
-                        const unsigned c = (unsigned)cols[a + k0 + u];
-                        v[u] = vals[a + k0 + u];
-                        // x is gathered through L2 only, so that the random
-                        // x lines do not evict the lanes' sequential row streams
-                        if (c < ncols) xv[u] = __ldcg(x + c);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < kSpAhead; ++u)
-                    if (k0 + u < L) acc = fma(v[u], xv[u], acc);
+            // x is gathered through L2 only, so that the random x lines do not
+            // evict the lanes' sequential row streams
+            auto xat = [&](unsigned c) { return c < ncols ? __ldcg(x + c) : 0.0; };
+            // entries one at a time until the columns are 16-byte aligned, then
+            // 4 per step: the columns by one 16-byte load, the values by two
+            // when they are 16-byte aligned too (the parity is fixed per row);
+            // the fma chain keeps the row's order throughout
+            int k = 0;
+            while (k < L && (reinterpret_cast<uintptr_t>(rc + k) & 15)) {
+                acc = fma(rv[k], xat((unsigned)rc[k]), acc);
+                ++k;
             }
+            const bool v16 = (reinterpret_cast<uintptr_t>(rv + k) & 15) == 0;
+            for (; k + 4 <= L; k += 4) {
+                const int4 c4 = *reinterpret_cast<const int4*>(rc + k);
+                double v0, v1, v2, v3;
+                if (v16) {
+                    const double2 p = *reinterpret_cast<const double2*>(rv + k);
+                    const double2 q = *reinterpret_cast<const double2*>(rv + k + 2);
+                    v0 = p.x; v1 = p.y; v2 = q.x; v3 = q.y;
+                } else {
+                    v0 = rv[k]; v1 = rv[k + 1]; v2 = rv[k + 2]; v3 = rv[k + 3];
+                }
+                const double x0 = xat((unsigned)c4.x), x1 = xat((unsigned)c4.y);
+                const double x2 = xat((unsigned)c4.z), x3 = xat((unsigned)c4.w);
+                acc = fma(v0, x0, acc);
+                acc = fma(v1, x1, acc);
+                acc = fma(v2, x2, acc);
+                acc = fma(v3, x3, acc);
+            }
+            for (; k < L; ++k) acc = fma(rv[k], xat((unsigned)rc[k]), acc);
             I.y[r0 + i] = acc;
         }
         __syncwarp();
