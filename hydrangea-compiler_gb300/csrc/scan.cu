@@ -90,6 +90,41 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* sh /*[32]*/, T& total)
     return r;
 }
 
+// The same for float64, without the subtraction the integer form uses for the
+// exclusive value (one FP64 operation fewer per thread; the FP64 pipe bounds
+// the float64 scan): the exclusive value of a lane is its left neighbour's
+// inclusive one.  Fixed order, so run-to-run identical.
+template <class T>
+__device__ __forceinline__ T block_exclusive_scan_shift(T v, T* sh /*[33]*/, T& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    T incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const T y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl = y + incl;
+    }
+    if (lane == 31) sh[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const T w = lane < nw ? sh[lane] : T(0);
+        T wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const T y = __shfl_up_sync(0xffffffffu, wi, d);
+            if (lane >= d) wi = y + wi;
+        }
+        const T wx = __shfl_up_sync(0xffffffffu, wi, 1);
+        sh[lane] = lane == 0 ? T(0) : wx;  // exclusive warp offsets
+        if (lane == 31) sh[32] = wi;
+    }
+    __syncthreads();
+    total = sh[32];
+    const T lx = __shfl_up_sync(0xffffffffu, incl, 1);
+    const T r = lane == 0 ? sh[warp] : sh[warp] + lx;
+    __syncthreads();
+    return r;
+}
+
 // Tile load/store in blocked arrangement through shared memory: global
 // accesses are coalesced, each thread then owns kScanIPT consecutive logical
 // elements.  Logical position k maps to physical index (reverse ? n-1-k : k).
@@ -308,11 +343,11 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_fold_kernel(const
     const int64_t base = (int64_t)tile * kScanTile;
     T items[kScanIPT];
     tile_load(in, n, base, reverse, sh_tile, items);
-    T tsum = items[0];
+    // the thread's running sums, in place: items[j] = x_0 + ... + x_j
 #pragma unroll
-    for (int j = 1; j < kScanIPT; ++j) tsum = tsum + items[j];
+    for (int j = 1; j < kScanIPT; ++j) items[j] = items[j - 1] + items[j];
     T agg;
-    const T texcl = block_exclusive_scan(tsum, sh_scan, agg);
+    const T texcl = block_exclusive_scan_shift(items[kScanIPT - 1], sh_scan, agg);
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
         const int64_t blk = tile >> 5;
@@ -346,17 +381,15 @@ __global__ void __launch_bounds__(kScanT, kScanCtasPerSm) scan_fold_kernel(const
         if (lane == 0) sh_prefix = pos == 0 ? before : before + within;
     }
     __syncthreads();
-    T acc = sh_prefix + texcl;
+    // outputs: the thread's prefix plus its running sums (one addition each)
+    const T p = sh_prefix + texcl;
+    if (inclusive) {
 #pragma unroll
-    for (int j = 0; j < kScanIPT; ++j) {
-        const T x = items[j];
-        if (inclusive) {
-            acc = acc + x;
-            items[j] = acc;
-        } else {
-            items[j] = acc;
-            acc = acc + x;
-        }
+        for (int j = 0; j < kScanIPT; ++j) items[j] = p + items[j];
+    } else {
+#pragma unroll
+        for (int j = kScanIPT - 1; j > 0; --j) items[j] = p + items[j - 1];
+        items[0] = p;
     }
     tile_store(out, n, base, reverse, sh_tile, items);
 }
