@@ -432,9 +432,12 @@ __global__ void __launch_bounds__(kWarps * 32, kBkWarpPerSm) bk_bucket_warp_kern
         for (int p = lane; p < E; p += 32) {
             const unsigned key = bk_key24(a[p], cbits);
             a[p] = key;
-            for (int k = 0; k < passes; ++k) {
-                const unsigned d = (key >> (8 * k)) & 0xFFu;
-                atomicAdd(&hist[k * 128 + (d & 127u)], (d & 128u) ? 0x10000u : 1u);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (k < passes) {
+                    const unsigned d = (key >> (8 * k)) & 0xFFu;
+                    atomicAdd(&hist[k * 128 + (d & 127u)], (d & 128u) ? 0x10000u : 1u);
+                }
             }
         }
         __syncwarp();
