@@ -407,8 +407,8 @@ __global__ void __launch_bounds__(kWarps * 32, kBkWarpPerSm) bk_bucket_warp_kern
         const BkInst I = inst[w.inst];
         const long long gb = I.bucket_base + w.tile;
         const int E = (int)bcount[gb];
-        int cbits = 0;
-        while ((1LL << cbits) < I.ncols) ++cbits;
+        // bits of the largest column: the smallest c with 2^c >= ncols
+        const int cbits = I.ncols > 1 ? 64 - __clzll((unsigned long long)(I.ncols - 1)) : 0;
         if (E > kCap || cbits > kBkWarpMaxCbits) {
             if (lane == 0) overflow[atomicAdd(overflow_count, 1u)] = w;
             continue;  // warp-uniform
